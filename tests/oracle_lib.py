@@ -1,0 +1,118 @@
+"""ctypes binding of the oracle (oracle/kg_oracle.c): test infrastructure.
+
+The oracle is the checker.  Only tests, the smoke check and bench.py's CPU
+baseline leg use it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+
+TESTS = ["laplacian", "divergence", "gradient", "uxx1", "wave13pt", "tricubic",
+         "tricubic2", "jacobi", "lapgsrb", "gaussblur", "gameoflife"]
+TEST_ID = {t: i for i, t in enumerate(TESTS)}
+NARR = [2, 4, 4, 6, 3, 5, 5, 2, 2, 2, 2]
+NCOEF = [2, 3, 3, 2, 3, 0, 0, 3, 4, 6, 0]
+IS2D = {"jacobi", "gaussblur", "gameoflife"}
+
+INIT_REFERENCE, INIT_BERNOULLI, INIT_UNIT_OFFSETS = 0, 1, 2
+
+
+class OrCase(ctypes.Structure):
+    _fields_ = [("test", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("ns", ctypes.c_int), ("narr", ctypes.c_int), ("ncoef", ctypes.c_int),
+                ("coef", ctypes.c_double * 6), ("arr", ctypes.c_void_p * 6),
+                ("order", ctypes.c_int * 6)]
+
+
+_libs = {}
+
+
+def load(flavour="strict"):
+    """Load build/liboracle.so (strict) or build/liboracle_fast.so (fast)."""
+    if flavour in _libs:
+        return _libs[flavour]
+    name = "liboracle.so" if flavour == "strict" else "liboracle_fast.so"
+    path = os.path.join(ORACLE_DIR, "build", name)
+    if not os.path.exists(path):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+    lib = ctypes.CDLL(path)
+    lib.or_init.argtypes = [ctypes.POINTER(OrCase), ctypes.c_int, ctypes.c_uint]
+    lib.or_sweep.argtypes = [ctypes.POINTER(OrCase)]
+    lib.or_run.argtypes = [ctypes.POINTER(OrCase), ctypes.c_int]
+    lib.or_initial_mean.argtypes = [ctypes.POINTER(OrCase)]
+    lib.or_initial_mean.restype = ctypes.c_double
+    lib.or_final_mean.argtypes = [ctypes.POINTER(OrCase)]
+    lib.or_final_mean.restype = ctypes.c_double
+    lib.or_final_slot.argtypes = [ctypes.POINTER(OrCase)]
+    lib.or_final_slot.restype = ctypes.c_int
+    lib.or_conway_u8.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.or_init_bernoulli_u8.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_double, ctypes.c_uint]
+    _libs[flavour] = lib
+    return lib
+
+
+class Case:
+    """A test program's state: arrays (numpy, float64) + coefficients."""
+
+    def __init__(self, test, shape, variant=INIT_REFERENCE, seed=1, flavour="strict"):
+        self.test = test
+        self.lib = load(flavour)
+        tid = TEST_ID[test]
+        if len(shape) == 2:
+            nx, ny, ns = shape[0], shape[1], 1
+        else:
+            nx, ny, ns = shape
+        self.shape = (nx, ny, ns)
+        n = nx * ny * ns
+        self.buffers = [np.zeros(n, dtype=np.float64) for _ in range(NARR[tid])]
+        self.c = OrCase()
+        self.c.test, self.c.nx, self.c.ny, self.c.ns = tid, nx, ny, ns
+        for q, b in enumerate(self.buffers):
+            self.c.arr[q] = b.ctypes.data
+        self.lib.or_init(ctypes.byref(self.c), variant, seed)
+
+    @property
+    def coef(self):
+        return [self.c.coef[q] for q in range(NCOEF[TEST_ID[self.test]])]
+
+    def arrays(self):
+        """Arrays in their current roles (slot order after rotation)."""
+        by_addr = {b.ctypes.data: b for b in self.buffers}
+        return [by_addr[self.c.arr[q]] for q in range(len(self.buffers))]
+
+    def sweep(self):
+        self.lib.or_sweep(ctypes.byref(self.c))
+
+    def run(self, nt):
+        self.lib.or_run(ctypes.byref(self.c), nt)
+
+    def initial_mean(self):
+        return self.lib.or_initial_mean(ctypes.byref(self.c))
+
+    def final_mean(self):
+        return self.lib.or_final_mean(ctypes.byref(self.c))
+
+    def final_slot(self):
+        return self.lib.or_final_slot(ctypes.byref(self.c))
+
+
+def conway_u8(u0, u1, nx, ny):
+    """One B3/S23 sweep u0 -> u1 (interior only; u1's rim is kept)."""
+    lib = load()
+    out = u1.copy()
+    lib.or_conway_u8(nx, ny, u0.ctypes.data, out.ctypes.data)
+    return out
+
+
+def bernoulli_u8(n, p=0.3, seed=1):
+    lib = load()
+    u0 = np.zeros(n, dtype=np.uint8)
+    u1 = np.zeros(n, dtype=np.uint8)
+    lib.or_init_bernoulli_u8(n, u0.ctypes.data, u1.ctypes.data, p, seed)
+    return u0, u1
