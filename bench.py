@@ -1,0 +1,458 @@
+#!/usr/bin/env python3
+"""Benchmark of the suite's stencil sweeps on GB300.
+
+Default workload (the suite in plain FP64, `benchmark 512 256 256 10`): one
+step runs all eleven stencils (laplacian, divergence, gradient, uxx1,
+wave13pt, tricubic, tricubic2, jacobi, lapgsrb, gaussblur, gameoflife), ten
+sweeps each with the reference's pointer rotation, 3D tests on 512x256x256
+and 2D tests on 512x65536, inputs drawn as the reference main() draws them
+(glibc rand(), default seed).  Metric: grid-point updates per second
+(Gpts/s, N = nx*ny*ns points per sweep, the reference's t_krn convention).
+
+  value   device-resident: arrays already in HBM, sweeps through kg_sweep.
+  e2e     the same steps through kg_program_run with pinned HOST arrays:
+          allocate, copy in, ten sweeps, copy the checksum arrays out, free.
+  --impl reference
+          the reference's CPU implementation of the sweeps (the oracle's C
+          restatement built with the suite's -O3 -ffast-math flags, OpenMP
+          over all host cores; the reference tree cannot be built on the GPU
+          host) on a bounded sample: one sweep of each stencil per step.
+
+Multi-GPU: the sweeps do not exchange data between problems; each rank runs
+an independent replica of the workload ("replicas only", weak scaling).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "kernelgen-perf-tests_gb300")
+sys.path.insert(0, PKG)
+
+import kgb200  # noqa: E402
+
+SUITE = kgb200.STENCILS
+SHAPE3 = (512, 256, 256)
+SHAPE2 = (512, 256 * 256)
+NT = 10
+NPTS = 512 * 256 * 256
+
+# Compulsory HBM bytes per point per sweep in FP64 (every input array read
+# once, every output array written once).
+BYTES_PER_PT = {"laplacian": 16, "divergence": 32, "gradient": 32, "uxx1": 48, "wave13pt": 24,
+                "tricubic": 40, "tricubic2": 40, "jacobi": 16, "lapgsrb": 16, "gaussblur": 16,
+                "gameoflife": 16}
+# FP64 operations per point in the reference expressions, counted after
+# common-subexpression elimination (tricubic: 12 weight products + 3 adds per
+# axis, 16 wa*wb, 64 *wc, 64 *u0, 63 adds); a division counts as one.
+FP64_OPS_PER_PT = {"laplacian": 8, "divergence": 8, "gradient": 6, "uxx1": 25, "wave13pt": 16,
+                   "tricubic": 252, "tricubic2": 253, "jacobi": 11, "lapgsrb": 28, "gaussblur": 31,
+                   "gameoflife": 14}
+# Arrays whose contents are the reference's checksum ("final mean") input.
+def result_mask(name):
+    return {"divergence": 0x1, "gradient": 0xE}.get(name, 0x2)
+
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# FP64 issue rate measured on this machine's GB300 with a DFMA/DADD throughput
+# kernel (profiles/gb300_fp64_rate.md): 0.505e12 FP64 operations per second.
+FP64_PEAK_OPS = 0.505e12
+# DRAM bytes per launch of the dominant kernel from ncu (see
+# profiles/suite_fp64_kernels.md); None until captured.
+NCU_TRAFFIC = {}
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---- inputs (the product's host code: the reference main()'s draws) -------
+
+_host = None
+
+
+def host_lib():
+    global _host
+    if _host is None:
+        _host = ctypes.CDLL(os.path.join(PKG, "build", "libkg_host.so"))
+        _host.kgh_init.argtypes = [ctypes.c_int] * 5 + [ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p]
+        _host.kgh_init.restype = None
+    return _host
+
+
+def shape_of(name):
+    return SHAPE2 if name in kgb200.IS2D else SHAPE3
+
+
+def make_inputs(names, variant=0, pinned=False):
+    """{name: (coef[6], [numpy float64 arrays])}, filled in parallel threads."""
+    import numpy as np
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+
+    out = {}
+
+    def one(name):
+        sh = shape_of(name)
+        nx, ny, ns = (sh[0], sh[1], 1) if len(sh) == 2 else sh
+        n = nx * ny * ns
+        narr = kgb200.load().kg_stencil_narrays(kgb200.STENCIL_ID[name])
+        if pinned:
+            ts = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(narr)]
+            arrs = [t.numpy() for t in ts]
+        else:
+            ts = None
+            arrs = [np.empty(n, dtype=np.float64) for _ in range(narr)]
+        coef = (ctypes.c_double * 6)()
+        ptrs = (ctypes.c_void_p * 6)(*[a.ctypes.data for a in arrs])
+        host_lib().kgh_init(kgb200.STENCIL_ID[name], nx, ny, ns, variant, 1, coef, ptrs)
+        return name, (list(coef), arrs, ts)
+
+    with ThreadPoolExecutor(max_workers=min(len(names), os.cpu_count() or 4)) as ex:
+        for name, v in ex.map(one, names):
+            out[name] = v
+    return out
+
+
+# ---- clocks -----------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- device-resident steps ------------------------------------------------
+
+def run_device(args, inputs, dtype):
+    import torch
+
+    stream = torch.cuda.current_stream()
+    sp = kgb200.stream_ptr(stream)
+    lib = kgb200.load()
+    probs = {}
+    keep = []
+    for name in SUITE:
+        coef, arrs, _ = inputs[name]
+        bufs = [torch.from_numpy(a).to("cuda") for a in arrs]
+        keep.append(bufs)
+        probs[name] = [kgb200.problem(name, dtype, shape_of(name), coef[:6], [b.data_ptr() for b in bufs])]
+        # the two-buffer / three-level rotations repeat with period 2 / 3
+        ptrs = [b.data_ptr() for b in bufs]
+        for _ in range(5):
+            ptrs = kgb200.rotate(name, ptrs)
+            probs[name].append(kgb200.problem(name, dtype, shape_of(name), coef[:6], ptrs))
+    torch.cuda.synchronize()
+
+    launches = {"n": 0}
+
+    def one_step(events=None):
+        for name in SUITE:
+            seq = probs[name]
+            for it in range(NT):
+                p = seq[it % len(seq)] if name not in ("divergence", "gradient") else seq[0]
+                if events is not None:
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                rc = lib.kg_sweep(ctypes.byref(p), sp)
+                if rc:
+                    kgb200.check(rc)
+                if events is not None:
+                    e1.record(stream)
+                    events[name].append((e0, e1))
+                launches["n"] += lib.kg_sweep_launches(p.stencil, p.dtype)
+        # each stencil's sequence continues where the step left it
+        for name in SUITE:
+            if name in ("divergence", "gradient"):
+                continue
+            period = 3 if name == "wave13pt" else 2
+            shift = NT % period
+            probs[name] = probs[name][shift:] + probs[name][:shift]
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    events = {n: [] for n in SUITE}
+    if args.world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches["n"] = 0
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_stop = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(args.local_rank) as clk:
+        t_start.record(stream)
+        for _ in range(args.steps):
+            one_step(events)
+        t_stop.record(stream)
+        torch.cuda.synchronize()
+    if args.world > 1:
+        dist.barrier()
+    total_ms = t_start.elapsed_time(t_stop)
+    per = {}
+    for name in SUITE:
+        ds = [a.elapsed_time(b) for a, b in events[name]]
+        per[name] = sum(ds) / len(ds)
+    finite = all(bool(torch.isfinite(b).all()) for bufs in keep for b in bufs)
+    del keep
+    torch.cuda.empty_cache()
+    return total_ms, per, clk.summary(), launches["n"], finite
+
+
+# ---- end to end through the C ABI with host buffers -----------------------
+
+def run_e2e(args, dtype):
+    import torch
+
+    inputs = make_inputs(SUITE, pinned=True)
+    stream = torch.cuda.current_stream()
+    h2d = d2h = 0
+    for name in SUITE:
+        coef, arrs, _ = inputs[name]
+        h2d += sum(a.nbytes for a in arrs)
+        d2h += bin(result_mask(name)).count("1") * arrs[0].nbytes
+
+    def step():
+        for name in SUITE:
+            coef, arrs, _ = inputs[name]
+            p = kgb200.problem(name, dtype, shape_of(name), coef[:6], [a.ctypes.data for a in arrs])
+            kgb200.program_run(p, NT, result_mask(name), stream)
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    del inputs
+    return dt, h2d, d2h
+
+
+# ---- CPU baseline (the oracle built with the suite's flags) ---------------
+
+def cpu_cases():
+    """The oracle's fast-math OpenMP build, set up on full-size inputs."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+
+    lib = ol.load("fast")
+    inputs = make_inputs(SUITE)
+    cases = {}
+    for name in SUITE:
+        coef, arrs, _ = inputs[name]
+        c = ol.OrCase()
+        sh = shape_of(name)
+        c.test = kgb200.STENCIL_ID[name]
+        c.nx, c.ny, c.ns = (sh[0], sh[1], 1) if len(sh) == 2 else sh
+        c.narr = len(arrs)
+        c.ncoef = ol.NCOEF[c.test]
+        for q in range(6):
+            c.coef[q] = coef[q]
+        for q, a in enumerate(arrs):
+            c.arr[q] = a.ctypes.data
+            c.order[q] = q
+        cases[name] = c
+    return lib, cases, inputs
+
+
+def cpu_sweeps(lib, cases, repeats=1, seconds_cap=1e9):
+    """Sweeps of each stencil at full size; returns (Gpts/s, threads, sample)."""
+    done = 0
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        for name in SUITE:
+            lib.or_sweep(ctypes.byref(cases[name]))
+            done += 1
+        if time.perf_counter() - t0 > seconds_cap:
+            break
+    dt = time.perf_counter() - t0
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    sample = "%d full-size sweeps (%d per stencil) of the 11 stencils, 512x256x256 / 512x65536, FP64" % (
+        done, done // len(SUITE))
+    return done * NPTS / dt / 1e9, threads, sample
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    lib, cases, keep = cpu_cases()
+    for _ in range(args.warmup):
+        cpu_sweeps(lib, cases, 1)
+    vals = []
+    for _ in range(args.steps):
+        g, threads, sample = cpu_sweeps(lib, cases, 1)
+        vals.append(g)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Gpts/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(11 * NPTS / (value * 1e9) * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": dict(CONFIG, sample="one sweep of each stencil per step (of the ten the workload runs)"),
+        "cpu_baseline": {"value": round(value, 4), "unit": "Gpts/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+METRIC = "Gpts/s, full suite plain FP64 (11 stencils x 10 sweeps, 512x256x256; 2D 512x65536)"
+DATA = "synthetic: the reference main()'s glibc rand() draws, default seed"
+CONFIG = {"workload": "suite-fp64 benchmark 512 256 256 10 (11 stencils x 10 sweeps per step)",
+          "shape_3d": list(SHAPE3), "shape_2d": list(SHAPE2), "sweeps_per_step": 11 * NT,
+          "points_per_sweep": NPTS, "l2": "no flush: every array (268 MB) is larger than L2 (129 MB)",
+          "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dtype", default="f64", choices=["f64", "f64fma"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.world, args.rank, args.local_rank = dist_env()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    if args.world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(args.local_rank)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    kgb200.check(kgb200.load().kg_device_check())
+    dtype = kgb200.DTYPES[args.dtype]
+
+    inputs = make_inputs(SUITE)
+    total_ms, per, clocks, launches, finite = run_device(args, inputs, dtype)
+    del inputs
+    if args.world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    pts_per_step = 11 * NT * NPTS
+    value = args.world * pts_per_step * args.steps / (total_ms * 1e-3) / 1e9
+    ms_per_step = total_ms / args.steps
+
+    # dominant kernel: the largest share of the step
+    share = {n: per[n] * NT for n in SUITE}
+    dom = max(share, key=share.get)
+    hbm, hbm_kind = peaks()
+    dur = per[dom] * 1e-3
+    achieved = BYTES_PER_PT[dom] * NPTS / dur / 1e9
+    fp64_ops = FP64_OPS_PER_PT[dom] * NPTS / dur
+    roofline = {
+        "kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+        "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_kind": hbm_kind,
+        "traffic": NCU_TRAFFIC.get(dom),
+        "bytes_per_launch": BYTES_PER_PT[dom] * NPTS, "launch_ms": round(per[dom], 4),
+        "fp64_alu": {"achieved_tops": round(fp64_ops / 1e12, 4), "peak_tops": FP64_PEAK_OPS / 1e12,
+                     "frac": round(fp64_ops / FP64_PEAK_OPS, 4),
+                     "note": "the FP64 sweeps are bound by GB300's FP64 issue rate, not HBM"},
+    }
+    per_stencil = {n: {"ms_per_sweep": round(per[n], 4), "gpts": round(NPTS / (per[n] * 1e-3) / 1e9, 2),
+                       "hbm_gbs": round(BYTES_PER_PT[n] * NPTS / (per[n] * 1e-3) / 1e9, 1),
+                       "fp64_tops": round(FP64_OPS_PER_PT[n] * NPTS / (per[n] * 1e-3) / 1e12, 4),
+                       "share": round(share[n] / sum(share.values()), 4)} for n in SUITE}
+
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "Gpts/s", "n_gpus": args.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": args.dtype, "data": DATA, "config": CONFIG, "roofline": roofline,
+        "gpu_launches": launches, "clocks": clocks, "finite": finite, "per_stencil": per_stencil,
+    }
+    if not args.no_e2e:
+        dt, h2d, d2h = run_e2e(args, dtype)
+        line["e2e"] = {"value": round(args.world * pts_per_step * args.steps / dt / 1e9, 4), "unit": "Gpts/s",
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "path": "kg_program_run per stencil: cudaMalloc, H2D, 10 sweeps, D2H of the checksum arrays, cudaFree"}
+    if args.rank == 0 and args.world == 1 and not args.no_cpu:
+        lib, cases, keep = cpu_cases()
+        g, threads, sample = cpu_sweeps(lib, cases, repeats=3, seconds_cap=25.0)
+        del keep
+        line["cpu_baseline"] = {"value": round(g, 4), "unit": "Gpts/s", "cores": threads, "kind": "port",
+                                "sample": sample}
+    if args.rank == 0:
+        print(json.dumps(line))
+    if args.world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

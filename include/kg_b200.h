@@ -1,0 +1,207 @@
+/*
+ * kg_b200.h -- C ABI of the GB300 (sm_103a) stencil-sweep library.
+ *
+ * Drop-in boundary for the kernel functions of kernelgen-perf-tests.  Each
+ * kg_<test>() replaces the reference kernel of the same name: same argument
+ * meaning and order, plus a storage/arithmetic type and a stream.  Pointers
+ * are device pointers owned by the caller; the call borrows them, launches
+ * one sweep asynchronously on `stream` and returns.  Unlike the reference
+ * (CUDA_SAFE_CALL prints and exit(-1), cuda_profiling.h:11-15) nothing here
+ * exits: every entry point returns a kg_status and kg_last_error() gives the
+ * message.  The caller performs the ping-pong pointer swap between sweeps, as
+ * the reference main() does (laplacian/laplacian.c:299-300).
+ *
+ * Layout: x fastest, element (i,j,k) at i + nx*j + nx*ny*k
+ * (laplacian/laplacian.c:30).  2D tests take (nx, ny) with ny the full row
+ * count (their makefiles pass NY*NS, gameoflife/gcc/makefile:45-46).
+ *
+ * Threading: calls are safe from several host threads on distinct streams;
+ * a kg_plan / kg_batch object is not thread-safe.
+ */
+#ifndef KG_B200_H
+#define KG_B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t; 0 is the legacy default stream. */
+typedef struct CUstream_st* kg_stream_t;
+
+typedef enum {
+	KG_OK = 0,
+	KG_EINVAL = 1,    /* bad argument: size, type, null or aliasing pointer */
+	KG_ECUDA = 2,     /* CUDA runtime error (see kg_last_error)              */
+	KG_ENOMEM = 3,    /* device or pinned-host allocation failed             */
+	KG_ETIMEOUT = 4,  /* an iteration cap or a bounded device wait ran out   */
+	KG_ENOTSUP = 5,   /* type not provided for this stencil                  */
+	KG_ENODEV = 6     /* no sm_103 device visible                            */
+} kg_status;
+
+/* Storage type of the arrays and the arithmetic used on them. */
+typedef enum {
+	KG_F64 = 0,      /* FP64, reference association order, no FMA contraction:
+	                    bitwise equal to an IEEE build of the reference kernel */
+	KG_F64_FMA = 1,  /* FP64, products contracted into FMA where the compiler
+	                    can (the suite's -ffast-math gcc build does the same)   */
+	KG_F32 = 2,      /* FP32 storage and arithmetic                           */
+	KG_BF16 = 3,     /* BF16 storage, FP32 arithmetic                         */
+	KG_F16 = 4,      /* FP16 storage, FP32 arithmetic                         */
+	KG_U8 = 5        /* 0/1 byte cells: gameoflife only (B3/S23)              */
+} kg_dtype;
+
+/* Stencil ids (the suite's test directories). */
+typedef enum {
+	KG_LAPLACIAN = 0, KG_DIVERGENCE = 1, KG_GRADIENT = 2, KG_UXX1 = 3,
+	KG_WAVE13PT = 4, KG_TRICUBIC = 5, KG_TRICUBIC2 = 6, KG_JACOBI = 7,
+	KG_LAPGSRB = 8, KG_GAUSSBLUR = 9, KG_GAMEOFLIFE = 10, KG_NSTENCILS = 11
+} kg_stencil;
+
+/* ---- one sweep per call (device pointers, asynchronous) ---------------- */
+
+/* laplacian/laplacian.c:44-50: w1 = alpha*w0 + beta*(6 faces), [1,n-2]^3. */
+kg_status kg_laplacian(kg_dtype dt, int nx, int ny, int ns, double alpha, double beta,
+	const void* w0, void* w1, kg_stream_t stream);
+
+/* divergence/divergence.c:44-50: u is written from ux, uy, uz, [1,n-2]^3. */
+kg_status kg_divergence(kg_dtype dt, int nx, int ny, int ns,
+	double alpha, double beta, double gamma,
+	void* u, const void* ux, const void* uy, const void* uz, kg_stream_t stream);
+
+/* gradient/gradient.c:45-51: ux, uy, uz are written from u, [1,n-2]^3. */
+kg_status kg_gradient(kg_dtype dt, int nx, int ny, int ns,
+	double alpha, double beta, double gamma,
+	const void* u, void* ux, void* uy, void* uz, kg_stream_t stream);
+
+/* uxx1/uxx1.c:45-51: u1 from u0, d1, xx, xy, xz; dth = 1/nx, [2,n-2]^3. */
+kg_status kg_uxx1(kg_dtype dt, int nx, int ny, int ns, double c1, double c2,
+	const void* u0, void* u1, const void* d1,
+	const void* xx, const void* xy, const void* xz, kg_stream_t stream);
+
+/* wave13pt/wave13pt.c:80-86: w2 from w0, w1 (13 points), [2,n-3]^3. */
+kg_status kg_wave13pt(kg_dtype dt, int nx, int ny, int ns,
+	double m0, double m1, double m2,
+	const void* w0, const void* w1, void* w2, kg_stream_t stream);
+
+/* tricubic/tricubic.c:71-77: u1 from u0 and offsets a, b, c, [1,n-3]^3. */
+kg_status kg_tricubic(kg_dtype dt, int nx, int ny, int ns,
+	const void* u0, void* u1, const void* a, const void* b, const void* c,
+	kg_stream_t stream);
+
+/* tricubic2/tricubic2.c:38-42: same maths accumulated from 0, [2,n-3]^3. */
+kg_status kg_tricubic2(kg_dtype dt, int nx, int ny, int ns,
+	const void* u0, void* u1, const void* a, const void* b, const void* c,
+	kg_stream_t stream);
+
+/* jacobi/jacobi.F90:15-19 (jacobi/main.c:43-52 binds it as jacobi_):
+ * 2D 9-point, 0-based interior [1,n-2]^2. */
+kg_status kg_jacobi(kg_dtype dt, int nx, int ny, double c0, double c1, double c2,
+	const void* w0, void* w1, kg_stream_t stream);
+
+/* lapgsrb/lapgsrb.c:44-50: 25-point out-of-place sweep, [2,n-3]^3. */
+kg_status kg_lapgsrb(kg_dtype dt, int nx, int ny, int ns,
+	double c0, double c1, double c2, double c3,
+	const void* w0, void* w1, kg_stream_t stream);
+
+/* gaussblur/gaussblur.c:44-50: 2D 5x5 blur, [2,n-3]^2. */
+kg_status kg_gaussblur(kg_dtype dt, int nx, int ny,
+	double s0, double s1, double s2, double s4, double s5, double s8,
+	const void* w0, void* w1, kg_stream_t stream);
+
+/* gameoflife/gameoflife.c:43-48: 2D smooth Conway on real cells (KG_F64,
+ * KG_F64_FMA, KG_F32) or B3/S23 on 0/1 byte cells (KG_U8), [1,n-2]^2. */
+kg_status kg_gameoflife(kg_dtype dt, int nx, int ny,
+	const void* u0, void* u1, kg_stream_t stream);
+
+/* ---- table-driven form of the same entry points ------------------------ */
+
+typedef struct {
+	int32_t stencil;     /* kg_stencil */
+	int32_t dtype;       /* kg_dtype   */
+	int32_t nx, ny, ns;  /* 2D stencils: ns = 1 */
+	int32_t reserved;
+	double coef[6];      /* coefficients in the reference's argument order */
+	void* arr[6];        /* arrays in the reference's argument order       */
+} kg_problem;
+
+int kg_stencil_narrays(int stencil);    /* -1 for an unknown id */
+int kg_stencil_ncoefs(int stencil);
+int kg_stencil_is2d(int stencil);
+/* Arrays a sweep writes, as a bit mask over kg_problem.arr. */
+int kg_stencil_outputs(int stencil);
+
+/* One sweep of p (device pointers). */
+kg_status kg_sweep(const kg_problem* p, kg_stream_t stream);
+
+/* ---- checksums (the reference's "initial mean" / "final mean") ---------- */
+
+/* out_dev[0] = sum over i of (a_0[i] + a_1[i] + ... + a_{narr-1}[i]) in FP64,
+ * narr <= 6, arrays of type dt with n elements each.  Deterministic: a fixed
+ * two-level tree, the same bits on every run.  Scratch (one double per block
+ * of the first level) comes from the stream-ordered pool. */
+kg_status kg_checksum(kg_dtype dt, size_t n, int narr, const void* const* arrays,
+	double* out_dev, kg_stream_t stream);
+
+/* Error of a low-precision result x (type dt) against an FP64 reference:
+ * out_dev[0] = max |x-ref|, [1] = sum (x-ref)^2, [2] = max |ref|,
+ * [3] = sum ref^2, all in FP64. */
+kg_status kg_error_stats(kg_dtype dt, size_t n, const void* x, const double* ref,
+	double* out_dev, kg_stream_t stream);
+
+/* Convert between storage types (FP64 <-> FP32/BF16/FP16, FP64 <-> U8 by
+ * threshold 0.5), elementwise. */
+kg_status kg_convert(kg_dtype dst_t, void* dst, kg_dtype src_t, const void* src,
+	size_t n, kg_stream_t stream);
+
+/* ---- whole test program on host arrays ---------------------------------- */
+
+typedef struct {
+	double alloc, load, compute, save, free_;  /* seconds, host wall clock   */
+	double kernel_avg;      /* mean device time of one sweep (CUDA events)  */
+	double kernel_min;
+	int nregs;              /* registers per thread of the sweep kernel     */
+	int reserved;
+} kg_timings;
+
+/* Phases 2-6 of the reference main() (laplacian/laplacian.c:222-370) for one
+ * test program: allocate device arrays, copy p->arr (HOST pointers) in, run
+ * nt sweeps with the reference's pointer rotation (two-buffer swap; wave13pt
+ * three-level rotation; divergence and gradient no swap), copy back the
+ * arrays selected by copy_back_mask (bit q = p->arr[q] in its final role),
+ * free.  On return p->arr holds the host arrays in their final roles, as the
+ * reference's idxs[] leaves them.  timings may be NULL. */
+kg_status kg_program_run(kg_problem* p, int nt, int copy_back_mask, kg_timings* timings,
+	kg_stream_t stream);
+
+/* ---- launch plans: the nt-sweep loop captured as one CUDA graph ---------- */
+
+typedef struct kg_plan_s* kg_plan;
+/* Records nt sweeps of p (device pointers) with the reference's rotation. */
+kg_status kg_plan_create(kg_plan* plan, const kg_problem* p, int nt);
+kg_status kg_plan_launch(kg_plan plan, kg_stream_t stream);
+/* After a launch: p->arr in their final roles. */
+kg_status kg_plan_final_roles(kg_plan plan, kg_problem* p);
+kg_status kg_plan_destroy(kg_plan plan);
+
+/* ---- introspection and errors ------------------------------------------ */
+
+/* Registers per thread of the kernel one sweep of (stencil, dt) launches. */
+kg_status kg_kernel_regcount(int stencil, kg_dtype dt, int* nregs);
+/* Kernel launches one sweep of (stencil, dt) makes (for launch counting). */
+int kg_sweep_launches(int stencil, kg_dtype dt);
+const char* kg_status_string(kg_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* kg_last_error(void);
+/* KG_OK if device 0 is an sm_103 GPU. */
+kg_status kg_device_check(void);
+/* Library version string. */
+const char* kg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KG_B200_H */

@@ -1,0 +1,212 @@
+// kg_ops.cuh -- the eleven stencil bodies, each in the reference's own term
+// and association order (see kg_num.cuh for why that makes KG_F64 bitwise).
+//
+// Every op declares its update domain as [L, n-1-H] per axis and reads its
+// inputs through `at(p, dx, dy, dz)`, an accessor centred on the point.  The
+// engine (kg_engine.cuh) supplies the accessor and the iteration.
+#pragma once
+
+#include "kg_num.cuh"
+
+namespace kg {
+
+// Slot roles in kg_problem.arr (reference argument order).
+struct Slots {
+	int in[6];
+	int nin;
+	int out[3];
+	int nout;
+};
+
+// laplacian/laplacian.c:81-97
+template <class N> struct OpLaplacian {
+	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 1, HZ = 1;
+	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	N alpha, beta;
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int w0 = 0;
+		o[0] = alpha * at(w0, 0, 0, 0) + beta * (
+			at(w0, 1, 0, 0) + at(w0, -1, 0, 0) +
+			at(w0, 0, 1, 0) + at(w0, 0, -1, 0) +
+			at(w0, 0, 0, 1) + at(w0, 0, 0, -1));
+	}
+};
+
+// divergence/divergence.c:84-97 (u written from ux, uy, uz)
+template <class N> struct OpDivergence {
+	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 1, HZ = 1;
+	static constexpr Slots slots() { return {{1, 2, 3}, 3, {0}, 1}; }
+	N alpha, beta, gamma;
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int ux = 0, uy = 1, uz = 2;
+		o[0] = alpha * (at(ux, 1, 0, 0) - at(ux, -1, 0, 0)) +
+		       beta  * (at(uy, 0, 1, 0) - at(uy, 0, -1, 0)) +
+		       gamma * (at(uz, 0, 0, 1) - at(uz, 0, 0, -1));
+	}
+};
+
+// gradient/gradient.c:85-98 (ux, uy, uz written from u)
+template <class N> struct OpGradient {
+	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 1, HZ = 1;
+	static constexpr Slots slots() { return {{0}, 1, {1, 2, 3}, 3}; }
+	N alpha, beta, gamma;
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int u = 0;
+		o[0] = alpha * (at(u, 1, 0, 0) - at(u, -1, 0, 0));
+		o[1] = beta  * (at(u, 0, 1, 0) - at(u, 0, -1, 0));
+		o[2] = gamma * (at(u, 0, 0, 1) - at(u, 0, 0, -1));
+	}
+};
+
+// uxx1/uxx1.c:70,83-106; dth = 1./nx is computed by the launcher (host IEEE
+// division, the same value as the reference's per-call computation).
+template <class N> struct OpUxx1 {
+	static constexpr int LX = 2, HX = 1, LY = 2, HY = 1, LZ = 2, HZ = 1;
+	static constexpr Slots slots() { return {{0, 2, 3, 4, 5}, 5, {1}, 1}; }
+	N c1, c2, dth;
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int u0 = 0, d1 = 1, xx = 2, xy = 3, xz = 4;
+		N d = N(0.25) * (
+			at(d1, 0, 0, 0) + at(d1, 0, -1, 0) +
+			at(d1, 0, 0, -1) + at(d1, 0, -1, -1));
+		o[0] = at(u0, 0, 0, 0) + (dth / d) * (
+			c1 * (at(xx, 0, 0, 0) - at(xx, -1, 0, 0)) +
+			c2 * (at(xx, 1, 0, 0) - at(xx, -2, 0, 0)) +
+			c1 * (at(xy, 0, 0, 0) - at(xy, 0, -1, 0)) +
+			c2 * (at(xy, 0, 1, 0) - at(xy, 0, -2, 0)) +
+			c1 * (at(xz, 0, 0, 0) - at(xz, 0, 0, -1)) +
+			c2 * (at(xz, 0, 0, 1) - at(xz, 0, 0, -2)));
+	}
+};
+
+// wave13pt/wave13pt.c:640-651 (plain branch), domain wave13pt.c:146-154,214
+template <class N> struct OpWave13pt {
+	static constexpr int LX = 2, HX = 2, LY = 2, HY = 2, LZ = 2, HZ = 2;
+	static constexpr Slots slots() { return {{0, 1}, 2, {2}, 1}; }
+	N m0, m1, m2;
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int w0 = 0, w1 = 1;
+		o[0] = m0 * at(w1, 0, 0, 0) - at(w0, 0, 0, 0) +
+			m1 * (
+				at(w1, 1, 0, 0) + at(w1, -1, 0, 0) +
+				at(w1, 0, 1, 0) + at(w1, 0, -1, 0) +
+				at(w1, 0, 0, 1) + at(w1, 0, 0, -1)) +
+			m2 * (
+				at(w1, 2, 0, 0) + at(w1, -2, 0, 0) +
+				at(w1, 0, 2, 0) + at(w1, 0, -2, 0) +
+				at(w1, 0, 0, 2) + at(w1, 0, 0, -2));
+	}
+};
+
+// tricubic/tricubic.c:1041-1054: cubic Lagrange weights, same association.
+template <class N> __device__ __forceinline__ void tricubic_weights(N a, N* w) {
+	const N one(1.0), two(2.0);
+	w[0] = N(1.0 / 6.0) * a * (a + one) * (a + two);
+	w[1] = N(-0.5) * (a - one) * (a + one) * (a + two);
+	w[2] = N(0.5) * (a - one) * a * (a + two);
+	w[3] = N(-1.0 / 6.0) * (a - one) * a * (a + one);
+}
+
+// tricubic/tricubic.c:1062-1145 (64 terms, t0 + t1 + ... + t63, x fastest)
+// and tricubic2/tricubic2.c:98-102 (u1 = 0; u1 += t_n, same term order).
+template <class N, bool FROM_ZERO> struct OpTricubicT {
+	static constexpr int LX = FROM_ZERO ? 2 : 1, HX = 2;
+	static constexpr int LY = FROM_ZERO ? 2 : 1, HY = 2;
+	static constexpr int LZ = FROM_ZERO ? 2 : 1, HZ = 2;
+	static constexpr Slots slots() { return {{0, 2, 3, 4}, 4, {1}, 1}; }
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int u0 = 0, pa = 1, pb = 2, pc = 3;
+		N wa[4], wb[4], wc[4];
+		tricubic_weights(at(pa, 0, 0, 0), wa);
+		tricubic_weights(at(pb, 0, 0, 0), wb);
+		tricubic_weights(at(pc, 0, 0, 0), wc);
+		N s;
+#pragma unroll
+		for (int kk = 0; kk < 4; kk++)
+#pragma unroll
+			for (int jj = 0; jj < 4; jj++)
+#pragma unroll
+				for (int ii = 0; ii < 4; ii++) {
+					N t = wa[ii] * wb[jj] * wc[kk] * at(u0, ii - 1, jj - 1, kk - 1);
+					if (kk == 0 && jj == 0 && ii == 0)
+						s = FROM_ZERO ? N(0.0) + t : t;
+					else
+						s = s + t;
+				}
+		o[0] = s;
+	}
+};
+template <class N> using OpTricubic = OpTricubicT<N, false>;
+template <class N> using OpTricubic2 = OpTricubicT<N, true>;
+
+// jacobi/jacobi.F90:60-67, Fortran (i,j) in [2,n-1] -> 0-based [1,n-2].
+template <class N> struct OpJacobi {
+	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 0, HZ = 0;
+	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	N c0, c1, c2;
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int w0 = 0;
+		o[0] = c0 * at(w0, 0, 0, 0) +
+			c1 * (at(w0, -1, 0, 0) + at(w0, 0, -1, 0) + at(w0, 1, 0, 0) + at(w0, 0, 1, 0)) +
+			c2 * (at(w0, -1, -1, 0) + at(w0, -1, 1, 0) + at(w0, 1, -1, 0) + at(w0, 1, 1, 0));
+	}
+};
+
+// lapgsrb/lapgsrb.c:93-117
+template <class N> struct OpLapgsrb {
+	static constexpr int LX = 2, HX = 2, LY = 2, HY = 2, LZ = 2, HZ = 2;
+	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	N c0, c1, c2, c3;
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int w = 0;
+		o[0] = c0 * at(w, 0, 0, 0) +
+			c1 * (
+				at(w, 1, 0, 0) + at(w, -1, 0, 0) +
+				at(w, 0, 1, 0) + at(w, 0, -1, 0) +
+				at(w, 0, 0, 1) + at(w, 0, 0, -1)) +
+			c2 * (
+				at(w, 1, 1, 0) + at(w, 1, 0, 1) + at(w, 1, 0, -1) + at(w, 1, -1, 0) +
+				at(w, 0, 1, 1) + at(w, 0, 1, -1) + at(w, 0, -1, 1) + at(w, 0, -1, -1) +
+				at(w, -1, 1, 0) + at(w, -1, 0, 1) + at(w, -1, 0, -1) + at(w, -1, -1, 0)) +
+			c3 * (
+				at(w, 2, 0, 0) + at(w, -2, 0, 0) +
+				at(w, 0, 2, 0) + at(w, 0, -2, 0) +
+				at(w, 0, 0, 2) + at(w, 0, 0, -2));
+	}
+};
+
+// gaussblur/gaussblur.c:65,85-92; f = 1/(s0+4(s1+s2+s4+s8)+8 s5) is computed
+// by the launcher (host, no contraction: the reference's per-call value).
+template <class N> struct OpGaussblur {
+	static constexpr int LX = 2, HX = 2, LY = 2, HY = 2, LZ = 0, HZ = 0;
+	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	N s0, s1, s2, s4, s5, s8, f;
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int w = 0;
+		o[0] = f * (
+			s0 *  at(w, 0, 0, 0) +
+			s1 * (at(w, -1, 0, 0) + at(w, 1, 0, 0) + at(w, 0, -1, 0) + at(w, 0, 1, 0)) +
+			s2 * (at(w, -1, -1, 0) + at(w, 1, -1, 0) + at(w, -1, 1, 0) + at(w, 1, 1, 0)) +
+			s4 * (at(w, -2, 0, 0) + at(w, 2, 0, 0) + at(w, 0, -2, 0) + at(w, 0, 2, 0)) +
+			s5 * (at(w, -2, -1, 0) + at(w, -1, -2, 0) + at(w, 1, -2, 0) + at(w, 2, -1, 0) +
+			      at(w, -2, 1, 0) + at(w, -1, 2, 0) + at(w, 1, 2, 0) + at(w, 2, 1, 0)) +
+			s8 * (at(w, -2, -2, 0) + at(w, 2, -2, 0) + at(w, -2, 2, 0) + at(w, 2, 2, 0)));
+	}
+};
+
+// gameoflife/gameoflife.c:81-91
+template <class N> struct OpGameoflife {
+	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 0, HZ = 0;
+	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
+		const int u0 = 0;
+		const N C(100000000000000000000.);
+		N L =
+			at(u0, -1, -1, 0) + at(u0, 0, -1, 0) + at(u0, 1, -1, 0) +
+			at(u0, -1, 0, 0)                     + at(u0, 1, 0, 0) +
+			at(u0, -1, 1, 0) + at(u0, 0, 1, 0) + at(u0, 1, 1, 0);
+		o[0] = N(1.) / (N(1.) + (at(u0, 0, 0, 0) + L - N(3.)) * (L - N(3.)) * C);
+	}
+};
+
+}  // namespace kg

@@ -1,0 +1,221 @@
+"""Python binding of the kg_b200 C ABI (include/kg_b200.h) over ctypes.
+
+The library is the in-tree build/libkg_b200.so of this package; there is no
+fallback: if it is missing or no sm_103 GPU is present, calls raise.
+Device memory is plain pointers (e.g. ``torch.Tensor.data_ptr()``).
+"""
+import ctypes
+import os
+import subprocess
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REPO_DIR = os.path.dirname(PKG_DIR)
+LIB_PATH = os.path.join(PKG_DIR, "build", "libkg_b200.so")
+HEADER = os.path.join(REPO_DIR, "include", "kg_b200.h")
+
+STENCILS = ["laplacian", "divergence", "gradient", "uxx1", "wave13pt", "tricubic",
+            "tricubic2", "jacobi", "lapgsrb", "gaussblur", "gameoflife"]
+STENCIL_ID = {s: i for i, s in enumerate(STENCILS)}
+IS2D = {"jacobi", "gaussblur", "gameoflife"}
+
+KG_F64, KG_F64_FMA, KG_F32, KG_BF16, KG_F16, KG_U8 = range(6)
+DTYPES = {"f64": KG_F64, "f64fma": KG_F64_FMA, "f32": KG_F32, "bf16": KG_BF16,
+          "f16": KG_F16, "u8": KG_U8}
+DTYPE_SIZE = {KG_F64: 8, KG_F64_FMA: 8, KG_F32: 4, KG_BF16: 2, KG_F16: 2, KG_U8: 1}
+STATUS = ["KG_OK", "KG_EINVAL", "KG_ECUDA", "KG_ENOMEM", "KG_ETIMEOUT", "KG_ENOTSUP", "KG_ENODEV"]
+
+# Every extern "C" symbol the header declares (checked by the CPU tests).
+EXPORTS = [
+    "kg_laplacian", "kg_divergence", "kg_gradient", "kg_uxx1", "kg_wave13pt", "kg_tricubic",
+    "kg_tricubic2", "kg_jacobi", "kg_lapgsrb", "kg_gaussblur", "kg_gameoflife",
+    "kg_stencil_narrays", "kg_stencil_ncoefs", "kg_stencil_is2d", "kg_stencil_outputs",
+    "kg_sweep", "kg_checksum", "kg_error_stats", "kg_convert", "kg_program_run",
+    "kg_plan_create", "kg_plan_launch", "kg_plan_final_roles", "kg_plan_destroy",
+    "kg_kernel_regcount", "kg_sweep_launches", "kg_status_string", "kg_last_error",
+    "kg_device_check", "kg_version",
+]
+
+
+class KgError(RuntimeError):
+    def __init__(self, status, msg):
+        self.status = status
+        name = STATUS[status] if 0 <= status < len(STATUS) else str(status)
+        super().__init__("%s: %s" % (name, msg))
+
+
+class KgProblem(ctypes.Structure):
+    _fields_ = [("stencil", ctypes.c_int32), ("dtype", ctypes.c_int32),
+                ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("ns", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("coef", ctypes.c_double * 6),
+                ("arr", ctypes.c_void_p * 6)]
+
+
+class KgTimings(ctypes.Structure):
+    _fields_ = [("alloc", ctypes.c_double), ("load", ctypes.c_double),
+                ("compute", ctypes.c_double), ("save", ctypes.c_double),
+                ("free_", ctypes.c_double), ("kernel_avg", ctypes.c_double),
+                ("kernel_min", ctypes.c_double), ("nregs", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
+
+
+def build(jobs=8, drivers=True, quiet=True):
+    """Compile build/libkg_b200.so (sm_103a) and the b200 target programs."""
+    targets = ["all"] + (["drivers"] if drivers else [])
+    out = subprocess.run(["make", "-j%d" % jobs, "-C", PKG_DIR] + targets,
+                         capture_output=quiet, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("build of %s failed:\n%s\n%s" % (PKG_DIR, out.stdout, out.stderr))
+
+
+_lib = None
+
+
+def _sig(lib):
+    P, I, D, S = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+    sig = {
+        "kg_laplacian": [I, I, I, I, D, D, P, P, P],
+        "kg_divergence": [I, I, I, I, D, D, D, P, P, P, P, P],
+        "kg_gradient": [I, I, I, I, D, D, D, P, P, P, P, P],
+        "kg_uxx1": [I, I, I, I, D, D, P, P, P, P, P, P, P],
+        "kg_wave13pt": [I, I, I, I, D, D, D, P, P, P, P],
+        "kg_tricubic": [I, I, I, I, P, P, P, P, P, P],
+        "kg_tricubic2": [I, I, I, I, P, P, P, P, P, P],
+        "kg_jacobi": [I, I, I, D, D, D, P, P, P],
+        "kg_lapgsrb": [I, I, I, I, D, D, D, D, P, P, P],
+        "kg_gaussblur": [I, I, I, D, D, D, D, D, D, P, P, P],
+        "kg_gameoflife": [I, I, I, P, P, P],
+        "kg_sweep": [ctypes.POINTER(KgProblem), P],
+        "kg_checksum": [I, S, I, ctypes.POINTER(ctypes.c_void_p), P, P],
+        "kg_error_stats": [I, S, P, P, P, P],
+        "kg_convert": [I, P, I, P, S, P],
+        "kg_program_run": [ctypes.POINTER(KgProblem), I, I, ctypes.POINTER(KgTimings), P],
+        "kg_plan_create": [ctypes.POINTER(P), ctypes.POINTER(KgProblem), I],
+        "kg_plan_launch": [P, P],
+        "kg_plan_final_roles": [P, ctypes.POINTER(KgProblem)],
+        "kg_plan_destroy": [P],
+        "kg_kernel_regcount": [I, I, ctypes.POINTER(I)],
+        "kg_device_check": [],
+    }
+    for name, args in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    for name in ("kg_stencil_narrays", "kg_stencil_ncoefs", "kg_stencil_is2d", "kg_stencil_outputs"):
+        getattr(lib, name).argtypes = [I]
+        getattr(lib, name).restype = I
+    lib.kg_sweep_launches.argtypes = [I, I]
+    lib.kg_sweep_launches.restype = I
+    for name in ("kg_status_string",):
+        getattr(lib, name).argtypes = [I]
+        getattr(lib, name).restype = ctypes.c_char_p
+    lib.kg_last_error.argtypes = []
+    lib.kg_last_error.restype = ctypes.c_char_p
+    lib.kg_version.argtypes = []
+    lib.kg_version.restype = ctypes.c_char_p
+
+
+def load():
+    """Load the in-tree library (no GPU needed to load it)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("%s is missing: run __graft_entry__.build()" % LIB_PATH)
+        lib = ctypes.CDLL(LIB_PATH)
+        _sig(lib)
+        _lib = lib
+    return _lib
+
+
+def check(status):
+    if status != 0:
+        raise KgError(status, load().kg_last_error().decode())
+
+
+def stream_ptr(stream):
+    """A torch.cuda.Stream (or None for the default stream) as kg_stream_t."""
+    if stream is None:
+        return None
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def problem(stencil, dtype, shape, coef, arrays):
+    """kg_problem from a stencil name, dtype id, shape, coefficients and device pointers."""
+    p = KgProblem()
+    p.stencil = STENCIL_ID[stencil] if isinstance(stencil, str) else int(stencil)
+    p.dtype = dtype
+    if len(shape) == 2:
+        p.nx, p.ny, p.ns = shape[0], shape[1], 1
+    else:
+        p.nx, p.ny, p.ns = shape
+    for q, c in enumerate(coef):
+        p.coef[q] = c
+    for q, a in enumerate(arrays):
+        p.arr[q] = a
+    return p
+
+
+def sweep(p, stream=None):
+    check(load().kg_sweep(ctypes.byref(p), stream_ptr(stream)))
+
+
+def checksum(dtype, n, arrays, out_ptr, stream=None):
+    arr = (ctypes.c_void_p * len(arrays))(*arrays)
+    check(load().kg_checksum(dtype, n, len(arrays), arr, out_ptr, stream_ptr(stream)))
+
+
+def error_stats(dtype, n, x_ptr, ref_ptr, out_ptr, stream=None):
+    check(load().kg_error_stats(dtype, n, x_ptr, ref_ptr, out_ptr, stream_ptr(stream)))
+
+
+def convert(dst_t, dst, src_t, src, n, stream=None):
+    check(load().kg_convert(dst_t, dst, src_t, src, n, stream_ptr(stream)))
+
+
+def regcount(stencil, dtype):
+    r = ctypes.c_int(0)
+    check(load().kg_kernel_regcount(STENCIL_ID.get(stencil, stencil), dtype, ctypes.byref(r)))
+    return r.value
+
+
+def rotate(stencil, arrays):
+    """The reference's pointer rotation after one sweep."""
+    a = list(arrays)
+    if stencil in ("divergence", "gradient"):
+        return a
+    if stencil == "wave13pt":
+        return [a[1], a[2], a[0]] + a[3:]
+    return [a[1], a[0]] + a[2:]
+
+
+class Plan:
+    """nt sweeps with the reference's rotation, captured as one CUDA graph."""
+
+    def __init__(self, p, nt):
+        self.h = ctypes.c_void_p()
+        check(load().kg_plan_create(ctypes.byref(self.h), ctypes.byref(p), nt))
+
+    def launch(self, stream=None):
+        check(load().kg_plan_launch(self.h, stream_ptr(stream)))
+
+    def final_roles(self):
+        p = KgProblem()
+        check(load().kg_plan_final_roles(self.h, ctypes.byref(p)))
+        return p
+
+    def close(self):
+        if self.h:
+            load().kg_plan_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def program_run(p, nt, copy_back_mask, stream=None):
+    """kg_program_run on host pointers; returns KgTimings (p.arr permuted in place)."""
+    t = KgTimings()
+    check(load().kg_program_run(ctypes.byref(p), nt, copy_back_mask, ctypes.byref(t), stream_ptr(stream)))
+    return t
