@@ -60,12 +60,10 @@ def result_mask(name):
 
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# FP64 issue rate measured on this machine's GB300 with a DFMA/DADD throughput
-# kernel (profiles/gb300_fp64_rate.md): 0.505e12 FP64 operations per second.
-FP64_PEAK_OPS = 0.505e12
-# DRAM bytes per launch of the dominant kernel from ncu (see
-# profiles/suite_fp64_kernels.md); None until captured.
-NCU_TRAFFIC = {}
+# DRAM bytes (read + write) per full-size launch from one ncu capture of a
+# smaller case scaled by the points processed (profiles/tricubic_f64_256x256x128.md,
+# profiles/laplacian_f64_256cube.md).
+NCU_TRAFFIC = {"tricubic": 4 * 312.8e6, "laplacian": 2 * 227.5e6}
 
 
 def peaks():
@@ -415,13 +413,14 @@ def main():
     dur = per[dom] * 1e-3
     achieved = BYTES_PER_PT[dom] * NPTS / dur / 1e9
     fp64_ops = FP64_OPS_PER_PT[dom] * NPTS / dur
+    fp64_peak = kgb200.measure_peaks().fp64_ops
     roofline = {
         "kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
         "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_kind": hbm_kind,
         "traffic": NCU_TRAFFIC.get(dom),
         "bytes_per_launch": BYTES_PER_PT[dom] * NPTS, "launch_ms": round(per[dom], 4),
-        "fp64_alu": {"achieved_tops": round(fp64_ops / 1e12, 4), "peak_tops": FP64_PEAK_OPS / 1e12,
-                     "frac": round(fp64_ops / FP64_PEAK_OPS, 4),
+        "fp64_alu": {"achieved_tops": round(fp64_ops / 1e12, 4), "peak_tops": round(fp64_peak / 1e12, 4),
+                     "frac": round(fp64_ops / fp64_peak, 4), "peak_kind": "measured live (kg_measure_peaks, DFMA)",
                      "note": "the FP64 sweeps are bound by GB300's FP64 issue rate, not HBM"},
     }
     per_stencil = {n: {"ms_per_sweep": round(per[n], 4), "gpts": round(NPTS / (per[n] * 1e-3) / 1e9, 2),

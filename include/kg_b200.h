@@ -188,6 +188,20 @@ kg_status kg_plan_destroy(kg_plan plan);
 
 /* ---- introspection and errors ------------------------------------------ */
 
+/* Arithmetic issue rates of the current device, measured with throughput
+ * kernels (operations per second; an FMA counts as one operation).  The FP64
+ * sweeps are bound by fp64_ops, the roofline denominator they report.
+ * No counterpart in the reference (its roofline rule uses nvprof metrics,
+ * wave13pt/cuda/makefile:57-66). */
+typedef struct {
+	double fp64_ops;    /* DFMA per second  */
+	double fp32_ops;    /* FFMA per second  */
+	double int32_ops;   /* IMAD per second  */
+	int sms;
+	int reserved;
+} kg_peaks;
+kg_status kg_measure_peaks(kg_peaks* out, kg_stream_t stream);
+
 /* Registers per thread of the kernel one sweep of (stencil, dt) launches. */
 kg_status kg_kernel_regcount(int stencil, kg_dtype dt, int* nregs);
 /* Kernel launches one sweep of (stencil, dt) makes (for launch counting). */

@@ -32,7 +32,7 @@ EXPORTS = [
     "kg_sweep", "kg_checksum", "kg_error_stats", "kg_convert", "kg_program_run",
     "kg_plan_create", "kg_plan_launch", "kg_plan_final_roles", "kg_plan_destroy",
     "kg_kernel_regcount", "kg_sweep_launches", "kg_status_string", "kg_last_error",
-    "kg_device_check", "kg_version",
+    "kg_device_check", "kg_version", "kg_measure_peaks",
 ]
 
 
@@ -48,6 +48,11 @@ class KgProblem(ctypes.Structure):
                 ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("ns", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("coef", ctypes.c_double * 6),
                 ("arr", ctypes.c_void_p * 6)]
+
+
+class KgPeaks(ctypes.Structure):
+    _fields_ = [("fp64_ops", ctypes.c_double), ("fp32_ops", ctypes.c_double),
+                ("int32_ops", ctypes.c_double), ("sms", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 class KgTimings(ctypes.Structure):
@@ -95,6 +100,7 @@ def _sig(lib):
         "kg_plan_destroy": [P],
         "kg_kernel_regcount": [I, I, ctypes.POINTER(I)],
         "kg_device_check": [],
+        "kg_measure_peaks": [ctypes.POINTER(KgPeaks), P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -212,6 +218,13 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def measure_peaks(stream=None):
+    """Measured FP64/FP32/INT32 issue rates of the current device (ops/s)."""
+    r = KgPeaks()
+    check(load().kg_measure_peaks(ctypes.byref(r), stream_ptr(stream)))
+    return r
 
 
 def program_run(p, nt, copy_back_mask, stream=None):
