@@ -145,6 +145,24 @@ kg_status kg_sweep(const kg_problem* p, kg_stream_t stream);
 kg_status kg_checksum(kg_dtype dt, size_t n, int narr, const void* const* arrays,
 	double* out_dev, kg_stream_t stream);
 
+/* kg_checksum for callers that cannot allocate device memory while they run:
+ * a host framework that owns all device memory through its own arena, or a
+ * latency-critical loop that cannot accept the synchronisation cudaMalloc /
+ * cudaFree may cause.  Same arguments, same first/second-level tree and so
+ * the same result bits as kg_checksum; no cudaMalloc, cudaFree or other
+ * allocating call.  The partial sums live in a fixed device array of
+ * KG_CHECKSUM_NOALLOC_PARTIALS doubles (16 KiB) that every GPU loading the
+ * library keeps until the process exits; n above KG_CHECKSUM_NOALLOC_MAX_N
+ * is rejected with KG_EINVAL.  The first call on each device looks up the
+ * array's device address (make it before any stream capture).  All calls
+ * share the array: calls whose kernels may overlap on the GPU (different
+ * streams without ordering) race and must be serialised by the caller.
+ * No counterpart in the reference. */
+#define KG_CHECKSUM_NOALLOC_PARTIALS 2048
+#define KG_CHECKSUM_NOALLOC_MAX_N ((size_t)1 << 33)
+kg_status kg_checksum_noalloc(kg_dtype dt, size_t n, int narr, const void* const* arrays,
+	double* out_dev, kg_stream_t stream);
+
 /* Error of a low-precision result x (type dt) against an FP64 reference:
  * out_dev[0] = max |x-ref|, [1] = sum (x-ref)^2, [2] = max |ref|,
  * [3] = sum ref^2, all in FP64. */

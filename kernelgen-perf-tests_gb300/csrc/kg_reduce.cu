@@ -11,6 +11,7 @@
 #include <cuda_fp16.h>
 
 #include <cstdint>
+#include <mutex>
 #include <type_traits>
 
 #include "kg_internal.h"
@@ -166,9 +167,91 @@ static cudaError_t convert_t(void* dst, const void* src, size_t n, cudaStream_t 
 	return cudaGetLastError();
 }
 
+// ---- kg_checksum_noalloc ------------------------------------------------------
+//
+// For callers that may not allocate device memory once they are running: a
+// host framework that hands out all device memory from its own arena, or a
+// latency-critical loop that cannot accept the device-wide synchronisation a
+// cudaMalloc/cudaFree may cause.  The partial sums live in this file-scope
+// array instead of the stream-ordered pool; every GPU that loads the library
+// holds its 16 KiB until the process exits.  Every call shares the array and
+// it keeps the previous call's partials: the first level writes every slot the
+// second level reads, so nothing has to be cleared, but two calls whose
+// kernels overlap on the GPU (different streams, no ordering between them)
+// race on it.
+static __device__ __align__(256) double g_checksum_partials[KG_CHECKSUM_NOALLOC_PARTIALS];
+static_assert(KG_CHECKSUM_NOALLOC_PARTIALS >= kRG, "the first level may use kRG partials");
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_partials_mu;
+static double* g_partials_addr[kMaxDevices];
+
+// The device address of g_checksum_partials on the current device.  In host
+// code the array's name stands for a host-side shadow, not device memory, so
+// its address is looked up once per device (with that device current) and
+// cached; the first call on a device does it.
+static kg_status partials_address(double** out)
+{
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return fail_cuda(e, "kg_checksum_noalloc: cudaGetDevice");
+	if (dev < 0 || dev >= kMaxDevices) return fail(KG_EINVAL, "kg_checksum_noalloc: device %d beyond %d", dev, kMaxDevices);
+	std::lock_guard<std::mutex> lock(g_partials_mu);
+	if (!g_partials_addr[dev]) {
+		void* p = nullptr;
+		e = cudaGetSymbolAddress(&p, g_checksum_partials);
+		if (e != cudaSuccess) return fail_cuda(e, "kg_checksum_noalloc: cudaGetSymbolAddress");
+		g_partials_addr[dev] = (double*)p;
+	}
+	*out = g_partials_addr[dev];
+	return KG_OK;
+}
+
+template <class S>
+static cudaError_t checksum_static_t(size_t n, const Arrs& A, double* partial, double* out, cudaStream_t st)
+{
+	const int g = reduce_blocks(n);
+	const size_t chunk = (n + g - 1) / g;
+	checksum_l1<S><<<g, kRB, 0, st>>>(A, n, chunk, partial);
+	reduce_l2<1><<<1, kRF, 0, st>>>(partial, g, out, 0);
+	return cudaGetLastError();
+}
+
 }  // namespace kg
 
 using namespace kg;
+
+extern "C" kg_status kg_checksum_noalloc(kg_dtype dt, size_t n, int narr, const void* const* arrays,
+	double* out_dev, kg_stream_t stream)
+{
+	clear_error();
+	if (narr < 1 || narr > 6 || !arrays || !out_dev)
+		return fail(KG_EINVAL, "kg_checksum_noalloc: narr must be 1..6, pointers non-null");
+	if (n > (size_t)KG_CHECKSUM_NOALLOC_MAX_N)
+		return fail(KG_EINVAL, "kg_checksum_noalloc: n = %zu exceeds the maximum of %zu elements",
+			n, (size_t)KG_CHECKSUM_NOALLOC_MAX_N);
+	Arrs A{};
+	A.narr = narr;
+	for (int q = 0; q < narr; q++) {
+		if (!arrays[q] && n) return fail(KG_EINVAL, "kg_checksum_noalloc: array %d is null", q);
+		A.a[q] = arrays[q];
+	}
+	cudaStream_t st = (cudaStream_t)stream;
+	if (n == 0) return fail_cuda(cudaMemsetAsync(out_dev, 0, sizeof(double), st), "kg_checksum_noalloc");
+	double* partial = nullptr;
+	kg_status s = partials_address(&partial);
+	if (s != KG_OK) return s;
+	cudaError_t e;
+	switch (dt) {
+	case KG_F64: case KG_F64_FMA: e = checksum_static_t<double>(n, A, partial, out_dev, st); break;
+	case KG_F32: e = checksum_static_t<float>(n, A, partial, out_dev, st); break;
+	case KG_BF16: e = checksum_static_t<__nv_bfloat16>(n, A, partial, out_dev, st); break;
+	case KG_F16: e = checksum_static_t<__half>(n, A, partial, out_dev, st); break;
+	case KG_U8: e = checksum_static_t<uint8_t>(n, A, partial, out_dev, st); break;
+	default: return fail(KG_EINVAL, "kg_checksum_noalloc: unknown dtype %d", (int)dt);
+	}
+	return fail_cuda(e, "kg_checksum_noalloc");
+}
 
 extern "C" kg_status kg_checksum(kg_dtype dt, size_t n, int narr, const void* const* arrays,
 	double* out_dev, kg_stream_t stream)

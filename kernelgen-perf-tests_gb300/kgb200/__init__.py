@@ -32,7 +32,7 @@ EXPORTS = [
     "kg_sweep", "kg_checksum", "kg_error_stats", "kg_convert", "kg_program_run",
     "kg_plan_create", "kg_plan_launch", "kg_plan_final_roles", "kg_plan_destroy",
     "kg_kernel_regcount", "kg_sweep_launches", "kg_status_string", "kg_last_error",
-    "kg_device_check", "kg_version", "kg_measure_peaks",
+    "kg_device_check", "kg_version", "kg_measure_peaks", "kg_checksum_noalloc",
 ]
 
 
@@ -91,6 +91,7 @@ def _sig(lib):
         "kg_gameoflife": [I, I, I, P, P, P],
         "kg_sweep": [ctypes.POINTER(KgProblem), P],
         "kg_checksum": [I, S, I, ctypes.POINTER(ctypes.c_void_p), P, P],
+        "kg_checksum_noalloc": [I, S, I, ctypes.POINTER(ctypes.c_void_p), P, P],
         "kg_error_stats": [I, S, P, P, P, P],
         "kg_convert": [I, P, I, P, S, P],
         "kg_program_run": [ctypes.POINTER(KgProblem), I, I, ctypes.POINTER(KgTimings), P],
