@@ -100,7 +100,7 @@ def shape_of(name):
     return SHAPE2 if name in kgb200.IS2D else SHAPE3
 
 
-def make_inputs(names, variant=0, pinned=False):
+def make_inputs(names, variant=0, pinned=False, shape=None):
     """{name: (coef[6], [numpy float64 arrays])}, filled in parallel threads."""
     import numpy as np
     import torch
@@ -109,7 +109,7 @@ def make_inputs(names, variant=0, pinned=False):
     out = {}
 
     def one(name):
-        sh = shape_of(name)
+        sh = shape or shape_of(name)
         nx, ny, ns = (sh[0], sh[1], 1) if len(sh) == 2 else sh
         n = nx * ny * ns
         narr = kgb200.load().kg_stencil_narrays(kgb200.STENCIL_ID[name])
@@ -261,6 +261,85 @@ def run_device(args, inputs, dtype):
     return total_ms, per, clk.summary(), launches["n"], finite
 
 
+# ---- precision sweep (wave13pt, uxx1; FP64 / FP32 / BF16) ------------------
+
+PRECISION_SHAPE = (1024, 512, 512)
+
+
+def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt", "uxx1")):
+    """The stencils advanced nsteps time steps from a Gaussian pulse (sigma 16
+    cells) + 1e-3 noise with stable coefficients, in FP64 (strict), FP32 and
+    BF16 storage with FP32 arithmetic, side by side.  Every `every` steps the
+    newest level of each narrow form is compared with FP64's (max and RMS of
+    the difference relative to max and RMS of the FP64 field) and its FP64
+    checksum taken.  Returns a dict per stencil."""
+    import numpy as np
+    import torch
+
+    nx, ny, ns = shape
+    n = nx * ny * ns
+    lib = kgb200.load()
+    stream = torch.cuda.current_stream()
+    sp = kgb200.stream_ptr(stream)
+    forms = [("f64", kgb200.KG_F64, torch.float64), ("f32", kgb200.KG_F32, torch.float32),
+             ("bf16", kgb200.KG_BF16, torch.bfloat16)]
+    out = {}
+    for name in names:
+        inputs = make_inputs([name], variant=3, shape=shape)
+        coef, arrs, _ = inputs[name]
+        f64 = [torch.from_numpy(a).to("cuda") for a in arrs]
+        del inputs, arrs
+        state = {}
+        for key, dt, tdt in forms:
+            bufs = f64 if key == "f64" else [t.to(tdt) for t in f64]
+            state[key] = {"dt": dt, "bufs": bufs, "ptrs": [b.data_ptr() for b in bufs], "ms": 0.0,
+                          "newest": None}
+        out_slot = 2 if name == "wave13pt" else 1
+        stats = torch.zeros(4, dtype=torch.float64, device="cuda")
+        sums = torch.zeros(1, dtype=torch.float64, device="cuda")
+        errs = {"f32": [], "bf16": []}
+        checks = {"f64": [], "f32": [], "bf16": []}
+        for block in range(nsteps // every):
+            for key, dt, _ in forms:
+                st = state[key]
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(every):
+                    p = kgb200.problem(name, dt, shape, coef[:6], st["ptrs"])
+                    kgb200.check(lib.kg_sweep(ctypes.byref(p), sp))
+                    st["newest"] = st["ptrs"][out_slot]
+                    st["ptrs"] = kgb200.rotate(name, st["ptrs"])
+                e1.record(stream)
+                torch.cuda.synchronize()
+                st["ms"] += e0.elapsed_time(e1)
+            step = (block + 1) * every
+            ref = state["f64"]["newest"]
+            for key, dt, _ in forms:
+                kgb200.checksum(dt, n, [state[key]["newest"]], sums.data_ptr(), stream)
+                checks[key].append(float(sums.item()) / n)
+                if key == "f64":
+                    continue
+                kgb200.error_stats(dt, n, state[key]["newest"], ref, stats.data_ptr(), stream)
+                mx, s2, mref, sref2 = stats.tolist()
+                errs[key].append([step, mx / mref if mref else 0.0,
+                                  (s2 / sref2) ** 0.5 if sref2 else 0.0])
+        res = {}
+        t64 = state["f64"]["ms"]
+        for key, dt, _ in forms:
+            ms = state[key]["ms"]
+            r = {"gpts": round(nsteps * n / (ms * 1e-3) / 1e9, 2), "ms_per_step": round(ms / nsteps, 4),
+                 "speedup_vs_f64": round(t64 / ms, 2), "mean_every_10": [float("%.9g" % c) for c in checks[key]]}
+            if key != "f64":
+                r["max_rel_err"] = [float("%.3g" % e[1]) for e in errs[key]]
+                r["rms_rel_err"] = [float("%.3g" % e[2]) for e in errs[key]]
+            res[key] = r
+        out[name] = res
+        del state, f64
+        torch.cuda.empty_cache()
+    return out
+
+
 # ---- end to end through the C ABI with host buffers -----------------------
 
 def run_e2e(args, dtype):
@@ -379,6 +458,8 @@ def main():
     ap.add_argument("--dtype", default="f64", choices=["f64", "f64fma"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the precision-sweep summary")
+    ap.add_argument("--workload", default="suite", choices=["suite", "precision"])
     args = ap.parse_args()
     args.world, args.rank, args.local_rank = dist_env()
     if args.impl == "reference":
@@ -393,6 +474,12 @@ def main():
         torch.cuda.set_device(0)
     kgb200.check(kgb200.load().kg_device_check())
     dtype = kgb200.DTYPES[args.dtype]
+    if args.workload == "precision":
+        res = run_precision()
+        if args.rank == 0:
+            print(json.dumps({"workload": "precision sweep wave13pt/uxx1 1024x512x512, 100 steps, "
+                              "Gaussian pulse sigma 16 + 1e-3 noise", "forms": res}))
+        return 0
 
     inputs = make_inputs(SUITE)
     total_ms, per, clocks, launches, finite = run_device(args, inputs, dtype)
@@ -440,6 +527,11 @@ def main():
         line["e2e"] = {"value": round(args.world * pts_per_step * args.steps / dt / 1e9, 4), "unit": "Gpts/s",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "path": "kg_program_run per stencil: cudaMalloc, H2D, 10 sweeps, D2H of the checksum arrays, cudaFree"}
+    if not args.no_forms:
+        line["forms"] = {"precision_sweep": dict(
+            workload="wave13pt and uxx1, 1024x512x512, 100 steps from a Gaussian pulse (sigma 16) + 1e-3 noise; "
+                     "FP64 strict vs FP32 and BF16 storage (FP32 arithmetic); errors relative to FP64 every 10 steps",
+            **run_precision())}
     if args.rank == 0 and args.world == 1 and not args.no_cpu:
         lib, cases, keep = cpu_cases()
         g, threads, sample = cpu_sweeps(lib, cases, repeats=3, seconds_cap=25.0)

@@ -109,12 +109,21 @@ void kgh_init(int test, int nx, int ny, int ns, int variant, unsigned seed,
 			coef[0] = 9.0 / 8.0;
 			coef[1] = -1.0 / 24.0;
 		}
-		for (size_t i = 0; i < n; i++) {
-			const double gp = pulse(nx, ny, ns, i);
-			for (int q = 0; q < narr; q++) {
-				double v = gp + 1e-3 * real_rand(g);
-				if (test == KG_UXX1 && q == 2) v = 1.0 + v;
-				arrs[q][i] = v;
+		/* The noise of plane k comes from its own generator, seeded with
+		 * seed + k + 1, so planes fill in parallel and the result does not
+		 * depend on the thread count. */
+		#pragma omp parallel for schedule(dynamic, 1)
+		for (int k = 0; k < ns; k++) {
+			kgh_rng pg;
+			kgh_rng_seed(&pg, seed + (unsigned)k + 1u);
+			const size_t i0 = (size_t)k * nx * ny, i1 = i0 + (size_t)nx * ny;
+			for (size_t i = i0; i < i1; i++) {
+				const double gp = pulse(nx, ny, ns, i);
+				for (int q = 0; q < narr; q++) {
+					double v = gp + 1e-3 * real_rand(&pg);
+					if (test == KG_UXX1 && q == 2) v = 1.0 + v;
+					arrs[q][i] = v;
+				}
 			}
 		}
 		return;

@@ -77,6 +77,26 @@ class Case:
             self.c.arr[q] = b.ctypes.data
         self.lib.or_init(ctypes.byref(self.c), variant, seed)
 
+    @classmethod
+    def from_arrays(cls, test, shape, coef, arrays, flavour="strict"):
+        """A case over given inputs (copied), e.g. the product's pulse input."""
+        self = cls.__new__(cls)
+        self.test = test
+        self.lib = load(flavour)
+        tid = TEST_ID[test]
+        nx, ny, ns = (shape[0], shape[1], 1) if len(shape) == 2 else shape
+        self.shape = (nx, ny, ns)
+        self.buffers = [np.array(a, dtype=np.float64, copy=True) for a in arrays]
+        self.c = OrCase()
+        self.c.test, self.c.nx, self.c.ny, self.c.ns = tid, nx, ny, ns
+        self.c.narr, self.c.ncoef = NARR[tid], NCOEF[tid]
+        for q, b in enumerate(self.buffers):
+            self.c.arr[q] = b.ctypes.data
+            self.c.order[q] = q
+        for q, v in enumerate(list(coef)[:6]):
+            self.c.coef[q] = v
+        return self
+
     @property
     def coef(self):
         return [self.c.coef[q] for q in range(NCOEF[TEST_ID[self.test]])]

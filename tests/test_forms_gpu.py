@@ -1,0 +1,76 @@
+"""The precision forms (precision-sweep input) against FP64 and the oracle.
+
+wave13pt and uxx1 advanced from the Gaussian-pulse input with stable
+coefficients: the strict FP64 run equals the oracle bit for bit; FP32 and
+BF16 storage (FP32 arithmetic) stay within the stated error of FP64.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+import kgb200  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+# Max-norm error of the narrow forms relative to max |FP64| within 30 steps.
+# The leapfrog wave update carries every rounding forward undamped, so its
+# error grows fastest (measured at 1024x512x512: FP32 1.2e-5 after 20 steps,
+# 1.1e-4 after 100; BF16 0.5 after 40); uxx1 accumulates linearly.
+TOL = {"wave13pt": {kgb200.KG_F32: 1e-4, kgb200.KG_BF16: 0.5},
+       "uxx1": {kgb200.KG_F32: 1e-5, kgb200.KG_BF16: 1e-2}}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+
+
+def pulse_inputs(name, shape):
+    host = ctypes.CDLL(os.path.join(ROOT, "kernelgen-perf-tests_gb300", "build", "libkg_host.so"))
+    nx, ny, ns = shape
+    narr = ol.NARR[ol.TEST_ID[name]]
+    arrs = [np.empty(nx * ny * ns) for _ in range(narr)]
+    coef = (ctypes.c_double * 6)()
+    ptrs = (ctypes.c_void_p * 6)(*[a.ctypes.data for a in arrs])
+    host.kgh_init(ol.TEST_ID[name], nx, ny, ns, 3, 1, coef, ptrs)
+    return list(coef), arrs
+
+
+@pytest.mark.parametrize("name", ["wave13pt", "uxx1"])
+def test_precision_sweep_small(name):
+    shape = (96, 64, 48)
+    coef, arrs = pulse_inputs(name, shape)
+    n = int(np.prod(shape))
+    case = ol.Case.from_arrays(name, shape, coef, arrs)
+    out_slot = 2 if name == "wave13pt" else 1
+    runs = {}
+    for dt, tdt in ((kgb200.KG_F64, torch.float64), (kgb200.KG_F32, torch.float32),
+                    (kgb200.KG_BF16, torch.bfloat16)):
+        bufs = [torch.from_numpy(a).cuda().to(tdt) for a in arrs]
+        runs[dt] = {"bufs": bufs, "ptrs": [b.data_ptr() for b in bufs]}
+    stats = torch.zeros(4, dtype=torch.float64, device="cuda")
+    for block in range(3):
+        newest = {}
+        for dt, r in runs.items():
+            for _ in range(10):
+                kgb200.sweep(kgb200.problem(name, dt, shape, coef, r["ptrs"]))
+                newest[dt] = r["ptrs"][out_slot]
+                r["ptrs"] = kgb200.rotate(name, r["ptrs"])
+        case.run(10)
+        torch.cuda.synchronize()
+        by = {b.data_ptr(): b for b in runs[kgb200.KG_F64]["bufs"]}
+        g = by[newest[kgb200.KG_F64]].cpu().numpy()
+        want = case.arrays()[1 if name == "wave13pt" else 0]
+        assert np.array_equal(g.view(np.uint64), want.view(np.uint64)), "FP64 differs from the oracle"
+        for dt in (kgb200.KG_F32, kgb200.KG_BF16):
+            kgb200.error_stats(dt, n, newest[dt], newest[kgb200.KG_F64], stats.data_ptr())
+            mx, s2, mref, sref2 = stats.tolist()
+            assert np.isfinite(mx) and mx / mref <= TOL[name][dt], (name, dt, block, mx / mref)
+        assert np.all(np.isfinite(g))
