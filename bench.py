@@ -340,6 +340,168 @@ def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt"
     return out
 
 
+# ---- batched uneven grids ----------------------------------------------------
+
+BATCH_KINDS = ["laplacian", "divergence", "wave13pt", "gaussblur"]
+
+
+def batch_specs(nprob=256, seed=2024):
+    """nx, ny, ns log-uniform in [32, 256], stencil uniform over BATCH_KINDS
+    (gaussblur as 2D nx x ny*ns).  Coefficients are drawn so that 50 steps
+    stay finite in FP32: laplacian beta and wave13pt m1, m2 in [-1/6, 1/6),
+    gaussblur weights in [0, 1) (its normaliser makes it a convex blur)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(nprob):
+        name = BATCH_KINDS[int(rng.integers(0, 4))]
+        nx, ny, ns = (int(round(float(np.exp(rng.uniform(np.log(32), np.log(256)))))) for _ in range(3))
+        shape = (nx, ny * ns) if name == "gaussblur" else (nx, ny, ns)
+        if name == "laplacian":
+            coef = [rng.uniform(-1, 1), rng.uniform(-1, 1) / 6]
+        elif name == "divergence":
+            coef = list(rng.uniform(-1, 1, 3))
+        elif name == "wave13pt":
+            coef = [rng.uniform(-1, 1), rng.uniform(-1, 1) / 6, rng.uniform(-1, 1) / 6]
+        else:
+            coef = list(rng.uniform(0, 1, 6))
+        specs.append((name, shape, [float(c) for c in coef]))
+    return specs
+
+
+def run_batched(nsteps=50, reps=3, tune_cache=None):
+    """256 problems, FP32 (inputs uniform [-1,1)): one persistent launch per
+    step in a captured 50-step CUDA graph, tuned tile shape and CTAs/SM,
+    against 256 sequential plain launches per step (host loop, and the same
+    launches captured in a graph), against the FP64 batch, and the FP32
+    result's error relative to FP64 after 50 steps."""
+    import torch
+
+    specs = batch_specs()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(2024)
+    lib = kgb200.load()
+    stream = torch.cuda.current_stream()
+    sp = kgb200.stream_ptr(stream)
+    init32, bufs32, bufs64 = [], [], []
+    npts = 0
+    for name, shape, coef in specs:
+        n = int(np_prod(shape))
+        npts += n
+        narr = lib.kg_stencil_narrays(kgb200.STENCIL_ID[name])
+        a = [torch.rand(n, generator=gen, device="cuda", dtype=torch.float32) * 2 - 1 for _ in range(narr)]
+        init32.append(a)
+        bufs32.append([x.clone() for x in a])
+        bufs64.append([x.double() for x in a])
+
+    def problems(dtype, bufs):
+        return [kgb200.problem(nm, dtype, sh, cf, [x.data_ptr() for x in b]) for (nm, sh, cf), b in zip(specs, bufs)]
+
+    def restore():
+        for b, a in zip(bufs32, init32):
+            for x, y in zip(b, a):
+                x.copy_(y)
+        for b, a in zip(bufs64, init32):
+            for x, y in zip(b, a):
+                x.copy_(y.double())
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, n=reps):
+        fn()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(n):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / n
+
+    out = {"problems": len(specs), "points_per_step": npts, "steps": nsteps,
+           "kinds": {k: sum(1 for s in specs if s[0] == k) for k in BATCH_KINDS}}
+    b32 = kgb200.Batch(problems(kgb200.KG_F32, bufs32))
+    t0 = time.perf_counter()
+    b32.tune(tune_cache, stream)
+    out["tune_s"] = round(time.perf_counter() - t0, 3)
+    cfg = b32.config()
+    out["tuned"] = {"bx": cfg.bx, "by": cfg.by, "kc": cfg.kc, "ctas_per_sm": cfg.ctas_per_sm, "tiles": cfg.tiles}
+    restore()
+    b32.set_step(0)
+    b32.capture(nsteps)
+    ms = timed(lambda: b32.launch(stream))
+    out["fp32_batched_graph_gpts"] = round(nsteps * npts / (ms * 1e-3) / 1e9, 2)
+    ms = timed(lambda: b32.step(nsteps, stream))
+    out["fp32_batched_launches_gpts"] = round(nsteps * npts / (ms * 1e-3) / 1e9, 2)
+
+    def sequential(dtype, bufs, steps):
+        sp = kgb200.stream_ptr(torch.cuda.current_stream())   # the capture stream inside a graph
+        ptrs = [[x.data_ptr() for x in b] for b in bufs]
+        for _ in range(steps):
+            for q, (nm, sh, cf) in enumerate(specs):
+                p = kgb200.problem(nm, dtype, sh, cf, ptrs[q])
+                rc = lib.kg_sweep(ctypes.byref(p), sp)
+                if rc:
+                    kgb200.check(rc)
+                ptrs[q] = kgb200.rotate(nm, ptrs[q])
+
+    ms = timed(lambda: sequential(kgb200.KG_F32, bufs32, nsteps), n=1)
+    out["fp32_sequential_host_gpts"] = round(nsteps * npts / (ms * 1e-3) / 1e9, 2)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        sequential(kgb200.KG_F32, bufs32, 6)   # 6 steps: a whole number of rotations
+    ms = timed(lambda: g.replay())
+    out["fp32_sequential_graph_gpts"] = round(6 * npts / (ms * 1e-3) / 1e9, 2)
+    del g
+
+    # FP64 (strict) batch and sequential, then errors after nsteps from the same inputs
+    b64 = kgb200.Batch(problems(kgb200.KG_F64, bufs64))
+    b64.set_config(cfg.shape, cfg.ctas_per_sm)
+    ms = timed(lambda: b64.step(6, stream), n=1)
+    out["fp64_batched_gpts"] = round(6 * npts / (ms * 1e-3) / 1e9, 2)
+    ms = timed(lambda: sequential(kgb200.KG_F64, bufs64, 6), n=1)
+    out["fp64_sequential_host_gpts"] = round(6 * npts / (ms * 1e-3) / 1e9, 2)
+    restore()
+    b32.set_step(0)
+    b64.set_step(0)
+    b32.launch(stream)
+    b64.step(nsteps, stream)
+    torch.cuda.synchronize()
+    stats = torch.zeros(4, dtype=torch.float64, device="cuda")
+    mx = s2 = mref = sref2 = 0.0
+    worst = 0.0
+    for q, (nm, sh, cf) in enumerate(specs):
+        p32, p64 = b32.final_roles(q), b64.final_roles(q)
+        slot = {"laplacian": 0, "gaussblur": 0, "wave13pt": 1, "divergence": 0}[nm]
+        n = int(np_prod(sh))
+        kgb200.error_stats(kgb200.KG_F32, n, p32.arr[slot], p64.arr[slot], stats.data_ptr(), stream)
+        a, b_, c, d = stats.tolist()
+        mx, s2, mref, sref2 = max(mx, a), s2 + b_, max(mref, c), sref2 + d
+        if c > 0:
+            worst = max(worst, a / c)
+    out["fp32_vs_fp64_after_%d_steps" % nsteps] = {
+        "max_rel": float("%.3g" % (mx / mref if mref else 0.0)),
+        "rms_rel": float("%.3g" % ((s2 / sref2) ** 0.5 if sref2 else 0.0)),
+        "worst_problem_max_rel": float("%.3g" % worst)}
+    out["speedup_batched_graph_vs_sequential_host"] = round(
+        out["fp32_batched_graph_gpts"] / out["fp32_sequential_host_gpts"], 2)
+    out["speedup_batched_graph_vs_sequential_graph"] = round(
+        out["fp32_batched_graph_gpts"] / out["fp32_sequential_graph_gpts"], 2)
+    out["speedup_fp32_batched_vs_fp64_sequential"] = round(
+        out["fp32_batched_graph_gpts"] / out["fp64_sequential_host_gpts"], 2)
+    b32.close()
+    b64.close()
+    del bufs32, bufs64, init32
+    torch.cuda.empty_cache()
+    return out
+
+
+def np_prod(shape):
+    r = 1
+    for v in shape:
+        r *= int(v)
+    return r
+
+
 # ---- end to end through the C ABI with host buffers -----------------------
 
 def run_e2e(args, dtype):
@@ -459,7 +621,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision-sweep summary")
-    ap.add_argument("--workload", default="suite", choices=["suite", "precision"])
+    ap.add_argument("--workload", default="suite", choices=["suite", "precision", "batched"])
     args = ap.parse_args()
     args.world, args.rank, args.local_rank = dist_env()
     if args.impl == "reference":
@@ -474,6 +636,12 @@ def main():
         torch.cuda.set_device(0)
     kgb200.check(kgb200.load().kg_device_check())
     dtype = kgb200.DTYPES[args.dtype]
+    if args.workload == "batched":
+        res = run_batched(tune_cache=os.environ.get("KG_TUNE_CACHE"))
+        if args.rank == 0:
+            print(json.dumps({"workload": "batched: 256 problems, log-uniform sizes in [32,256], "
+                              "{laplacian, divergence, wave13pt, gaussblur}, FP32, 50 steps", "forms": res}))
+        return 0
     if args.workload == "precision":
         res = run_precision()
         if args.rank == 0:
@@ -532,6 +700,7 @@ def main():
             workload="wave13pt and uxx1, 1024x512x512, 100 steps from a Gaussian pulse (sigma 16) + 1e-3 noise; "
                      "FP64 strict vs FP32 and BF16 storage (FP32 arithmetic); errors relative to FP64 every 10 steps",
             **run_precision())}
+        line["forms"]["batched"] = run_batched(tune_cache=os.environ.get("KG_TUNE_CACHE"))
     if args.rank == 0 and args.world == 1 and not args.no_cpu:
         lib, cases, keep = cpu_cases()
         g, threads, sample = cpu_sweeps(lib, cases, repeats=3, seconds_cap=25.0)

@@ -204,6 +204,42 @@ kg_status kg_plan_launch(kg_plan plan, kg_stream_t stream);
 kg_status kg_plan_final_roles(kg_plan plan, kg_problem* p);
 kg_status kg_plan_destroy(kg_plan plan);
 
+/* ---- batches: many uneven problems, one persistent launch per step ------ */
+
+/* Up to 4096 independent problems of laplacian, divergence, wave13pt and
+ * gaussblur (2D, ns = 1), all KG_F32 or all KG_F64, advanced together.  Each
+ * step is one persistent kernel launch over the tiles of every problem; each
+ * problem's arrays rotate their roles per step as the reference loops do.
+ * Results equal nsteps kg_sweep calls per problem, bit for bit.
+ * No counterpart in the reference (each suite program runs one problem). */
+typedef struct kg_batch_s* kg_batch;
+typedef struct {
+	int shape, bx, by, kc;   /* tile shape: BX x BY threads, KC planes (rows in 2D) */
+	int ctas_per_sm;
+	int tiles;               /* tiles of all problems per step */
+	int nshapes;             /* tile shapes the tuner tries */
+	int reserved;
+	long long steps_done;
+} kg_batch_config;
+kg_status kg_batch_create(kg_batch* b, const kg_problem* probs, int nprob);
+/* Launches nsteps steps on the stream. */
+kg_status kg_batch_step(kg_batch b, int nsteps, kg_stream_t stream);
+/* Captures nsteps steps (plus the step-counter advance) as a CUDA graph;
+ * kg_batch_launch replays it and continues from the current step. */
+kg_status kg_batch_capture(kg_batch b, int nsteps);
+kg_status kg_batch_launch(kg_batch b, kg_stream_t stream);
+/* Times every tile shape x {2,4,8} CTAs/SM on this batch (advancing it) and
+ * keeps the fastest; cache_path (may be NULL) stores and reuses the choice
+ * per device and problem list. */
+kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream);
+kg_status kg_batch_set_config(kg_batch b, int shape, int ctas_per_sm);
+kg_status kg_batch_get_config(kg_batch b, kg_batch_config* cfg);
+/* Sets the step count (roles restart from step 0 with 0). */
+kg_status kg_batch_set_step(kg_batch b, long long step);
+/* Problem q with its arrays in the reference's roles after the steps done. */
+kg_status kg_batch_final_roles(kg_batch b, int q, kg_problem* out);
+kg_status kg_batch_destroy(kg_batch b);
+
 /* ---- introspection and errors ------------------------------------------ */
 
 /* Arithmetic issue rates of the current device, measured with throughput

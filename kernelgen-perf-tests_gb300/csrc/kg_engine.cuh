@@ -30,43 +30,84 @@ template <class N, class S> struct GAcc {
 
 constexpr int kBX = 32, kBY = 8;
 
-template <class Op, class N, class S, int KC>
-__global__ void __launch_bounds__(kBX * kBY) sweep_kernel(Op op, Ptrs<S> p, int nx, int ny, int ns)
+// One tile: BX x BY columns (threadIdx.x, threadIdx.y) of the update domain,
+// planes [LZ + tz*KC, LZ + (tz+1)*KC).  2D ops (LZ = HZ = 0, ns = 1) walk KC
+// rows instead, BY apart, so a tile covers BX x (BY*KC) points either way.
+template <class Op, class N, class S, int BX, int BY, int KC>
+__device__ __forceinline__ void sweep_tile(const Op& op, const Ptrs<S>& p, int nx, int ny, int ns,
+	int tx, int ty, int tz)
 {
 	constexpr Slots sl = Op::slots();
-	const int i = Op::LX + blockIdx.x * kBX + threadIdx.x;
-	const int iend = nx - Op::HX, jend = ny - Op::HY, kend = ns - Op::HZ;
-	if (i >= iend) return;
+	constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
+	const int i = Op::LX + tx * BX + (int)threadIdx.x;
+	if (i >= nx - Op::HX) return;
 	const long long sy = nx, sz = (long long)nx * ny;
-	for (int j = Op::LY + blockIdx.y * kBY + threadIdx.y; j < jend; j += gridDim.y * kBY) {
-		for (int k0 = Op::LZ + blockIdx.z * KC; k0 < kend; k0 += gridDim.z * KC) {
-			const int k1 = min(k0 + KC, kend);
-			for (int k = k0; k < k1; k++) {
-				const long long c = i + sy * j + sz * k;
-				GAcc<N, S> at{p.in, c, sy, sz};
-				N o[3];
-				op.point(at, o);
+	if (k2d) {
+		const int j0 = Op::LY + ty * (BY * KC) + (int)threadIdx.y;
+#pragma unroll 1
+		for (int r = 0; r < KC; r++) {
+			const int j = j0 + r * BY;
+			if (j >= ny - Op::HY) break;
+			const long long c = i + sy * j;
+			GAcc<N, S> at{p.in, c, sy, sz};
+			N o[3];
+			op.point(at, o);
 #pragma unroll
-				for (int q = 0; q < sl.nout; q++) p.out[q][c] = Conv<N, S>::to(o[q]);
-			}
+			for (int q = 0; q < sl.nout; q++) p.out[q][c] = Conv<N, S>::to(o[q]);
+		}
+	} else {
+		const int j = Op::LY + ty * BY + (int)threadIdx.y;
+		if (j >= ny - Op::HY) return;
+		const int k0 = Op::LZ + tz * KC, k1 = min(k0 + KC, ns - Op::HZ);
+#pragma unroll 1
+		for (int k = k0; k < k1; k++) {
+			const long long c = i + sy * j + sz * k;
+			GAcc<N, S> at{p.in, c, sy, sz};
+			N o[3];
+			op.point(at, o);
+#pragma unroll
+			for (int q = 0; q < sl.nout; q++) p.out[q][c] = Conv<N, S>::to(o[q]);
 		}
 	}
 }
 
+// Tiles of a domain along each axis for the (BX, BY, KC) tile shape.
+template <class Op> struct TileCount {
+	static __host__ __device__ int x(int nx, int bx) { return max(0, (nx - Op::LX - Op::HX + bx - 1) / bx); }
+	static __host__ __device__ int y(int ny, int by, int kc) {
+		const int d = ny - Op::LY - Op::HY;
+		const int t = (Op::LZ == 0 && Op::HZ == 0) ? by * kc : by;
+		return max(0, (d + t - 1) / t);
+	}
+	static __host__ __device__ int z(int ns, int kc) {
+		if (Op::LZ == 0 && Op::HZ == 0) return 1;
+		return max(0, (ns - Op::LZ - Op::HZ + kc - 1) / kc);
+	}
+};
+
+template <class Op, class N, class S, int KC>
+__global__ void __launch_bounds__(kBX * kBY) sweep_kernel(Op op, Ptrs<S> p, int nx, int ny, int ns)
+{
+	const int tyn = TileCount<Op>::y(ny, kBY, KC), tzn = TileCount<Op>::z(ns, KC);
+	for (int ty = blockIdx.y; ty < tyn; ty += gridDim.y)
+		for (int tz = blockIdx.z; tz < tzn; tz += gridDim.z)
+			sweep_tile<Op, N, S, kBX, kBY, KC>(op, p, nx, ny, ns, blockIdx.x, ty, tz);
+}
+
 template <class Op, class N, class S>
 struct Launch {
-	static constexpr int KC = (Op::LZ == 0 && Op::HZ == 0) ? 1 : 8;
+	static constexpr int KC = 8;
 	static const void* func() { return (const void*)sweep_kernel<Op, N, S, KC>; }
 	static cudaError_t run(const Op& op, const kg_problem& pr, cudaStream_t st) {
 		constexpr Slots sl = Op::slots();
 		Ptrs<S> p{};
 		for (int q = 0; q < sl.nin; q++) p.in[q] = (const S*)pr.arr[sl.in[q]];
 		for (int q = 0; q < sl.nout; q++) p.out[q] = (S*)pr.arr[sl.out[q]];
-		const int dx = pr.nx - Op::LX - Op::HX, dy = pr.ny - Op::LY - Op::HY, dz = pr.ns - Op::LZ - Op::HZ;
-		if (dx <= 0 || dy <= 0 || dz <= 0) return cudaSuccess;  // empty domain: nothing to write
+		const int tx = TileCount<Op>::x(pr.nx, kBX), ty = TileCount<Op>::y(pr.ny, kBY, KC),
+			tz = TileCount<Op>::z(pr.ns, KC);
+		if (tx <= 0 || ty <= 0 || tz <= 0) return cudaSuccess;  // empty domain: nothing to write
 		dim3 block(kBX, kBY, 1);
-		dim3 grid((dx + kBX - 1) / kBX, (unsigned)min((dy + kBY - 1) / kBY, 65535),
-			(unsigned)min((dz + KC - 1) / KC, 65535));
+		dim3 grid(tx, (unsigned)min(ty, 65535), (unsigned)min(tz, 65535));
 		sweep_kernel<Op, N, S, KC><<<grid, block, 0, st>>>(op, p, pr.nx, pr.ny, pr.ns);
 		return cudaGetLastError();
 	}

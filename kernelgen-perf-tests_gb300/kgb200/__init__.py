@@ -33,6 +33,9 @@ EXPORTS = [
     "kg_plan_create", "kg_plan_launch", "kg_plan_final_roles", "kg_plan_destroy",
     "kg_kernel_regcount", "kg_sweep_launches", "kg_status_string", "kg_last_error",
     "kg_device_check", "kg_version", "kg_measure_peaks", "kg_checksum_noalloc",
+    "kg_batch_create", "kg_batch_step", "kg_batch_capture", "kg_batch_launch", "kg_batch_tune",
+    "kg_batch_set_config", "kg_batch_get_config", "kg_batch_set_step", "kg_batch_final_roles",
+    "kg_batch_destroy",
 ]
 
 
@@ -53,6 +56,12 @@ class KgProblem(ctypes.Structure):
 class KgPeaks(ctypes.Structure):
     _fields_ = [("fp64_ops", ctypes.c_double), ("fp32_ops", ctypes.c_double),
                 ("int32_ops", ctypes.c_double), ("sms", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+class KgBatchConfig(ctypes.Structure):
+    _fields_ = [("shape", ctypes.c_int), ("bx", ctypes.c_int), ("by", ctypes.c_int), ("kc", ctypes.c_int),
+                ("ctas_per_sm", ctypes.c_int), ("tiles", ctypes.c_int), ("nshapes", ctypes.c_int),
+                ("reserved", ctypes.c_int), ("steps_done", ctypes.c_longlong)]
 
 
 class KgTimings(ctypes.Structure):
@@ -102,6 +111,16 @@ def _sig(lib):
         "kg_kernel_regcount": [I, I, ctypes.POINTER(I)],
         "kg_device_check": [],
         "kg_measure_peaks": [ctypes.POINTER(KgPeaks), P],
+        "kg_batch_create": [ctypes.POINTER(P), ctypes.POINTER(KgProblem), I],
+        "kg_batch_step": [P, I, P],
+        "kg_batch_capture": [P, I],
+        "kg_batch_launch": [P, P],
+        "kg_batch_tune": [P, ctypes.c_char_p, P],
+        "kg_batch_set_config": [P, I, I],
+        "kg_batch_get_config": [P, ctypes.POINTER(KgBatchConfig)],
+        "kg_batch_set_step": [P, ctypes.c_longlong],
+        "kg_batch_final_roles": [P, I, ctypes.POINTER(KgProblem)],
+        "kg_batch_destroy": [P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -226,6 +245,55 @@ def measure_peaks(stream=None):
     r = KgPeaks()
     check(load().kg_measure_peaks(ctypes.byref(r), stream_ptr(stream)))
     return r
+
+
+class Batch:
+    """kg_batch: many problems (list of KgProblem, device pointers) stepped together."""
+
+    def __init__(self, problems):
+        arr = (KgProblem * len(problems))(*problems)
+        self.n = len(problems)
+        self.h = ctypes.c_void_p()
+        check(load().kg_batch_create(ctypes.byref(self.h), arr, len(problems)))
+
+    def step(self, nsteps=1, stream=None):
+        check(load().kg_batch_step(self.h, nsteps, stream_ptr(stream)))
+
+    def capture(self, nsteps):
+        check(load().kg_batch_capture(self.h, nsteps))
+
+    def launch(self, stream=None):
+        check(load().kg_batch_launch(self.h, stream_ptr(stream)))
+
+    def tune(self, cache_path=None, stream=None):
+        check(load().kg_batch_tune(self.h, cache_path.encode() if cache_path else None, stream_ptr(stream)))
+
+    def set_config(self, shape, ctas):
+        check(load().kg_batch_set_config(self.h, shape, ctas))
+
+    def config(self):
+        c = KgBatchConfig()
+        check(load().kg_batch_get_config(self.h, ctypes.byref(c)))
+        return c
+
+    def set_step(self, step):
+        check(load().kg_batch_set_step(self.h, step))
+
+    def final_roles(self, q):
+        p = KgProblem()
+        check(load().kg_batch_final_roles(self.h, q, ctypes.byref(p)))
+        return p
+
+    def close(self):
+        if self.h:
+            load().kg_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def program_run(p, nt, copy_back_mask, stream=None):
