@@ -495,6 +495,62 @@ def run_batched(nsteps=50, reps=3, tune_cache=None):
     return out
 
 
+# ---- mixed-precision iterative refinement (Poisson) -------------------------
+
+IR_SHAPE = (768, 768, 512)
+IR_SMALL = (192, 192, 128)
+
+
+def run_ir(shape=IR_SMALL, rtol=1e-10, omega=1.8, per_check=100, fp64_cap=None, kinds=None):
+    """A u = f, 7-point Laplacian, u = 0 on the outer planes, f uniform
+    [-1,1) on the interior with its mean removed: time to ||f - A u|| <=
+    rtol ||f|| for plain FP64 red-black SOR and for FP64 refinement around
+    FP32 red-black SOR (and Jacobi, where it is given the sweeps)."""
+    import torch
+
+    nx, ny, ns = shape
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(5)
+    f = torch.zeros((ns, ny, nx), dtype=torch.float64, device="cuda")
+    inner = torch.rand((ns - 2, ny - 2, nx - 2), generator=gen, device="cuda", dtype=torch.float64) * 2 - 1
+    f[1:-1, 1:-1, 1:-1] = inner - inner.mean()
+    del inner
+    f = f.reshape(-1)
+    npts = nx * ny * ns
+    out = {"shape": list(shape), "rtol": rtol, "omega": omega, "sweeps_per_check": per_check}
+    kinds = kinds or [("fp64_sor", kgb200.KG_SOLVE_SOR_F64, fp64_cap),
+                      ("ir_fp32_sor", kgb200.KG_SOLVE_IR_SOR_F32, None)]
+    for key, kind, cap in kinds:
+        u = torch.zeros_like(f)
+        torch.cuda.synchronize()
+        st, rep = kgb200.poisson_solve(shape, f.data_ptr(), u.data_ptr(), kind, omega=omega, rtol=rtol,
+                                       sweeps_per_check=per_check, max_sweeps=cap or 10**7,
+                                       raise_on_timeout=False)
+        r = {"status": kgb200.STATUS[st], "sweeps": rep.sweeps, "seconds": round(rep.seconds, 3),
+             "rel_residual": float("%.3g" % rep.rel_residual), "outer": rep.outer,
+             "ms_per_sweep": round(rep.seconds * 1e3 / max(rep.sweeps, 1), 4),
+             "gpts": round(rep.sweeps * npts / max(rep.seconds, 1e-9) / 1e9, 2)}
+        hist = [(rep.history_sweeps[i], rep.history_rel[i]) for i in range(rep.nhistory)]
+        if st == 4 and len(hist) >= 3:
+            # capped: project the time to tolerance from the measured rate of the last half
+            import math
+            (s0, r0), (s1, r1) = hist[len(hist) // 2], hist[-1]
+            if r1 < r0 and s1 > s0:
+                rate = (math.log(r0) - math.log(r1)) / (s1 - s0)
+                need = s1 + (math.log(r1) - math.log(rtol)) / rate
+                r["projected_sweeps"] = int(need)
+                r["projected_seconds"] = round(need * rep.seconds / rep.sweeps, 2)
+        out[key] = r
+        del u
+    base = out["fp64_sor"]
+    t64 = base.get("projected_seconds", base["seconds"]) if base["status"] != "KG_OK" else base["seconds"]
+    for key in list(out):
+        if isinstance(out[key], dict) and key != "fp64_sor" and out[key].get("status") == "KG_OK":
+            out[key]["speedup_vs_fp64_sor"] = round(t64 / out[key]["seconds"], 2)
+    torch.cuda.empty_cache()
+    return out
+
+
 def np_prod(shape):
     r = 1
     for v in shape:
@@ -621,7 +677,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision-sweep summary")
-    ap.add_argument("--workload", default="suite", choices=["suite", "precision", "batched"])
+    ap.add_argument("--workload", default="suite", choices=["suite", "precision", "batched", "ir"])
+    ap.add_argument("--ir-shape", default="768,768,512")
+    ap.add_argument("--ir-fp64-cap", type=int, default=0, help="sweep cap of the FP64 SOR run (0: none)")
     args = ap.parse_args()
     args.world, args.rank, args.local_rank = dist_env()
     if args.impl == "reference":
@@ -636,6 +694,12 @@ def main():
         torch.cuda.set_device(0)
     kgb200.check(kgb200.load().kg_device_check())
     dtype = kgb200.DTYPES[args.dtype]
+    if args.workload == "ir":
+        shape = tuple(int(v) for v in args.ir_shape.split(","))
+        res = run_ir(shape, fp64_cap=args.ir_fp64_cap or None)
+        if args.rank == 0:
+            print(json.dumps({"workload": "mixed-precision iterative refinement, Poisson 7-point", "forms": res}))
+        return 0
     if args.workload == "batched":
         res = run_batched(tune_cache=os.environ.get("KG_TUNE_CACHE"))
         if args.rank == 0:
@@ -701,6 +765,9 @@ def main():
                      "FP64 strict vs FP32 and BF16 storage (FP32 arithmetic); errors relative to FP64 every 10 steps",
             **run_precision())}
         line["forms"]["batched"] = run_batched(tune_cache=os.environ.get("KG_TUNE_CACHE"))
+        line["forms"]["iterative_refinement"] = dict(
+            note="measured to tolerance on 192x192x128; the 768x768x512 run is bench.py --workload ir",
+            **run_ir(IR_SMALL))
     if args.rank == 0 and args.world == 1 and not args.no_cpu:
         lib, cases, keep = cpu_cases()
         g, threads, sample = cpu_sweeps(lib, cases, repeats=3, seconds_cap=25.0)

@@ -240,6 +240,38 @@ kg_status kg_batch_set_step(kg_batch b, long long step);
 kg_status kg_batch_final_roles(kg_batch b, int q, kg_problem* out);
 kg_status kg_batch_destroy(kg_batch b);
 
+/* ---- Poisson solves: red-black SOR, mixed-precision iterative refinement -- */
+
+/* A u = f with the 7-point Laplacian (A u = 6 u - sum of the 6 face
+ * neighbours), u = 0 on the outer planes, f and u FP64 on the device (u holds
+ * the initial guess and receives the solution).  KG_SOLVE_SOR_F64: red-black
+ * SOR in FP64.  KG_SOLVE_IR_*_F32: FP64 residual and correction around FP32
+ * red-black SOR or Jacobi sweeps.  Stops when ||f - A u||_2 <= rtol ||f||_2
+ * (checked every sweeps_per_check sweeps) or returns KG_ETIMEOUT after
+ * max_sweeps.  No counterpart in the reference (its lapgsrb is an out-of-
+ * place 25-point sweep, lapgsrb/lapgsrb.c:81-117, not red-black SOR). */
+enum { KG_SOLVE_SOR_F64 = 0, KG_SOLVE_IR_SOR_F32 = 1, KG_SOLVE_IR_JACOBI_F32 = 2 };
+#define KG_SOLVE_HISTORY 256
+typedef struct {
+	int kind;
+	int sweeps_per_check;
+	double omega;          /* SOR relaxation factor, 0 < omega < 2 */
+	double rtol;           /* relative residual target */
+	long long max_sweeps;
+} kg_solve_opts;
+typedef struct {
+	long long sweeps;      /* relaxation sweeps done (one red + one black half each) */
+	int outer;             /* refinement steps (FP64 corrections) */
+	int nhistory;
+	double rel_residual;   /* final ||f - A u|| / ||f|| */
+	double fnorm;
+	double seconds;        /* host wall clock of the solve */
+	long long history_sweeps[KG_SOLVE_HISTORY];
+	double history_rel[KG_SOLVE_HISTORY];
+} kg_solve_report;
+kg_status kg_poisson_solve(int nx, int ny, int ns, const double* f, double* u,
+	const kg_solve_opts* opts, kg_solve_report* report, kg_stream_t stream);
+
 /* ---- introspection and errors ------------------------------------------ */
 
 /* Arithmetic issue rates of the current device, measured with throughput

@@ -35,8 +35,9 @@ EXPORTS = [
     "kg_device_check", "kg_version", "kg_measure_peaks", "kg_checksum_noalloc",
     "kg_batch_create", "kg_batch_step", "kg_batch_capture", "kg_batch_launch", "kg_batch_tune",
     "kg_batch_set_config", "kg_batch_get_config", "kg_batch_set_step", "kg_batch_final_roles",
-    "kg_batch_destroy",
+    "kg_batch_destroy", "kg_poisson_solve",
 ]
+KG_SOLVE_SOR_F64, KG_SOLVE_IR_SOR_F32, KG_SOLVE_IR_JACOBI_F32 = 0, 1, 2
 
 
 class KgError(RuntimeError):
@@ -62,6 +63,17 @@ class KgBatchConfig(ctypes.Structure):
     _fields_ = [("shape", ctypes.c_int), ("bx", ctypes.c_int), ("by", ctypes.c_int), ("kc", ctypes.c_int),
                 ("ctas_per_sm", ctypes.c_int), ("tiles", ctypes.c_int), ("nshapes", ctypes.c_int),
                 ("reserved", ctypes.c_int), ("steps_done", ctypes.c_longlong)]
+
+
+class KgSolveOpts(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("sweeps_per_check", ctypes.c_int), ("omega", ctypes.c_double),
+                ("rtol", ctypes.c_double), ("max_sweeps", ctypes.c_longlong)]
+
+
+class KgSolveReport(ctypes.Structure):
+    _fields_ = [("sweeps", ctypes.c_longlong), ("outer", ctypes.c_int), ("nhistory", ctypes.c_int),
+                ("rel_residual", ctypes.c_double), ("fnorm", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("history_sweeps", ctypes.c_longlong * 256), ("history_rel", ctypes.c_double * 256)]
 
 
 class KgTimings(ctypes.Structure):
@@ -121,6 +133,7 @@ def _sig(lib):
         "kg_batch_set_step": [P, ctypes.c_longlong],
         "kg_batch_final_roles": [P, I, ctypes.POINTER(KgProblem)],
         "kg_batch_destroy": [P],
+        "kg_poisson_solve": [I, I, I, P, P, ctypes.POINTER(KgSolveOpts), ctypes.POINTER(KgSolveReport), P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -294,6 +307,18 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def poisson_solve(shape, f_ptr, u_ptr, kind, omega=1.8, rtol=1e-10, sweeps_per_check=100,
+                  max_sweeps=10**7, stream=None, raise_on_timeout=True):
+    """kg_poisson_solve; returns (status, KgSolveReport)."""
+    o = KgSolveOpts(kind, sweeps_per_check, omega, rtol, max_sweeps)
+    r = KgSolveReport()
+    nx, ny, ns = shape
+    st = load().kg_poisson_solve(nx, ny, ns, f_ptr, u_ptr, ctypes.byref(o), ctypes.byref(r), stream_ptr(stream))
+    if st != 0 and (raise_on_timeout or st != 4):
+        check(st)
+    return st, r
 
 
 def program_run(p, nt, copy_back_mask, stream=None):

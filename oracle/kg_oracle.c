@@ -11,6 +11,7 @@
  */
 #include "kg_oracle.h"
 
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -380,6 +381,37 @@ void or_run(or_case* c, int nt)
 			swap_slots(c, 0, 1); break;
 		}
 	}
+}
+
+void or_rbsor_sweep(int nx, int ny, int ns, double omega, double* u, const double* f)
+{
+	for (int color = 0; color < 2; color++)
+		for (int k = 1; k < ns - 1; k++)
+			for (int j = 1; j < ny - 1; j++)
+				for (int i = 1; i < nx - 1; i++)
+				{
+					if (((i + j + k) & 1) != color) continue;
+					const size_t c = IX(i, j, k);
+					const double s = u[c - 1] + u[c + 1] + u[c - nx] + u[c + nx] +
+						u[c - (size_t)nx * ny] + u[c + (size_t)nx * ny];
+					u[c] = u[c] + omega * ((s + f[c]) * (1.0 / 6.0) - u[c]);
+				}
+}
+
+double or_residual_norm(int nx, int ny, int ns, const double* u, const double* f)
+{
+	double acc = 0.0;
+	for (int k = 1; k < ns - 1; k++)
+		for (int j = 1; j < ny - 1; j++)
+			for (int i = 1; i < nx - 1; i++)
+			{
+				const size_t c = IX(i, j, k);
+				const double au = 6.0 * u[c] - (u[c - 1] + u[c + 1] + u[c - nx] + u[c + nx] +
+					u[c - (size_t)nx * ny] + u[c + (size_t)nx * ny]);
+				const double r = f[c] - au;
+				acc += r * r;
+			}
+	return sqrt(acc);
 }
 
 double or_sum(const double* x, size_t n)

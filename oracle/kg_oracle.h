@@ -104,6 +104,14 @@ double or_final_mean(const or_case* c);
  * tests: the input of the last sweep; wave13pt: the newest level). */
 int or_final_slot(const or_case* c);
 
+/* Red-black SOR for A u = f, A u = 6 u - (6 face neighbours), u = 0 on the
+ * outer planes: one sweep = the red half ((i+j+k) even) then the black half,
+ * u += omega * ((sum + f) / 6 - u).  Project-defined (PARITY UNPINNED: the
+ * reference has no such solver; checked by its residual). */
+void or_rbsor_sweep(int nx, int ny, int ns, double omega, double* u, const double* f);
+/* ||f - A u||_2 over the interior. */
+double or_residual_norm(int nx, int ny, int ns, const double* u, const double* f);
+
 /* Plain FP64 serial sum of x[0..n). */
 double or_sum(const double* x, size_t n);
 

@@ -53,8 +53,25 @@ def load(flavour="strict"):
     lib.or_conway_u8.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.or_init_bernoulli_u8.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_double, ctypes.c_uint]
+    lib.or_rbsor_sweep.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_void_p, ctypes.c_void_p]
+    lib.or_residual_norm.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.or_residual_norm.restype = ctypes.c_double
     _libs[flavour] = lib
     return lib
+
+
+def rbsor_sweeps(u, f, shape, omega, nsweeps):
+    lib = load()
+    nx, ny, ns = shape
+    for _ in range(nsweeps):
+        lib.or_rbsor_sweep(nx, ny, ns, omega, u.ctypes.data, f.ctypes.data)
+    return u
+
+
+def residual_norm(u, f, shape):
+    nx, ny, ns = shape
+    return load().or_residual_norm(nx, ny, ns, u.ctypes.data, f.ctypes.data)
 
 
 class Case:

@@ -1,0 +1,95 @@
+"""Poisson solves (config: mixed-precision iterative refinement).
+
+The solver is project-defined (the reference has no red-black SOR): its
+oracle is the CPU restatement of the red-black SOR sweep in oracle/ plus the
+residual itself, computed on the CPU in FP64 from the returned solution.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+import kgb200  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device():
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+
+
+def poisson_rhs(shape, seed=7):
+    """f uniform [-1,1) on the interior with its mean removed, 0 on the outer planes."""
+    nx, ny, ns = shape
+    rng = np.random.default_rng(seed)
+    f = np.zeros((ns, ny, nx))
+    inner = rng.uniform(-1, 1, (ns - 2, ny - 2, nx - 2))
+    f[1:-1, 1:-1, 1:-1] = inner - inner.mean()
+    return f.reshape(-1)
+
+
+def test_sor_sweeps_match_oracle():
+    shape = (21, 18, 16)
+    f = poisson_rhs(shape)
+    u_cpu = np.zeros_like(f)
+    ol.rbsor_sweeps(u_cpu, f, shape, 1.8, 30)
+    fd = torch.from_numpy(f).cuda()
+    ud = torch.zeros_like(fd)
+    st, rep = kgb200.poisson_solve(shape, fd.data_ptr(), ud.data_ptr(), kgb200.KG_SOLVE_SOR_F64,
+                                   rtol=1e-30, sweeps_per_check=30, max_sweeps=30, raise_on_timeout=False)
+    assert st == 4 and rep.sweeps == 30          # capped: KG_ETIMEOUT, no hang
+    u = ud.cpu().numpy()
+    assert np.max(np.abs(u - u_cpu)) <= 1e-13 * np.max(np.abs(u_cpu))
+
+
+@pytest.mark.parametrize("kind", [kgb200.KG_SOLVE_SOR_F64, kgb200.KG_SOLVE_IR_SOR_F32])
+def test_solve_to_tolerance(kind):
+    shape = (40, 36, 30)
+    f = poisson_rhs(shape)
+    fd = torch.from_numpy(f).cuda()
+    ud = torch.zeros_like(fd)
+    st, rep = kgb200.poisson_solve(shape, fd.data_ptr(), ud.data_ptr(), kind, omega=1.8, rtol=1e-10,
+                                   sweeps_per_check=25)
+    assert st == 0 and rep.rel_residual <= 1e-10
+    u = ud.cpu().numpy()
+    rel = ol.residual_norm(u, f, shape) / np.linalg.norm(f)
+    assert rel <= 1.05e-10, rel
+    # the boundary stays zero
+    g = u.reshape(shape[2], shape[1], shape[0])
+    assert not g[0].any() and not g[-1].any() and not g[:, 0].any() and not g[:, :, -1].any()
+
+
+def test_refinement_keeps_the_sor_rate():
+    """Refinement with FP32 inner SOR needs about as many sweeps as FP64 SOR."""
+    shape = (48, 40, 32)
+    f = poisson_rhs(shape)
+    fd = torch.from_numpy(f).cuda()
+    res = {}
+    for kind in (kgb200.KG_SOLVE_SOR_F64, kgb200.KG_SOLVE_IR_SOR_F32):
+        ud = torch.zeros_like(fd)
+        st, rep = kgb200.poisson_solve(shape, fd.data_ptr(), ud.data_ptr(), kind, rtol=1e-10, sweeps_per_check=20)
+        assert st == 0
+        res[kind] = rep.sweeps
+    assert res[kgb200.KG_SOLVE_IR_SOR_F32] <= 1.15 * res[kgb200.KG_SOLVE_SOR_F64] + 20
+
+
+def test_jacobi_refinement_converges():
+    shape = (14, 12, 10)
+    f = poisson_rhs(shape)
+    fd = torch.from_numpy(f).cuda()
+    ud = torch.zeros_like(fd)
+    st, rep = kgb200.poisson_solve(shape, fd.data_ptr(), ud.data_ptr(), kgb200.KG_SOLVE_IR_JACOBI_F32,
+                                   rtol=1e-10, sweeps_per_check=200, max_sweeps=200000)
+    assert st == 0
+    rel = ol.residual_norm(ud.cpu().numpy(), f, shape) / np.linalg.norm(f)
+    assert rel <= 1.05e-10
+
+
+def test_solve_rejects_bad_options():
+    fd = torch.zeros(27, dtype=torch.float64, device="cuda")
+    with pytest.raises(kgb200.KgError):
+        kgb200.poisson_solve((3, 3, 3), fd.data_ptr(), fd.data_ptr(), 7)
+    with pytest.raises(kgb200.KgError):
+        kgb200.poisson_solve((3, 3, 3), fd.data_ptr(), fd.data_ptr(), 0, omega=2.5)
