@@ -185,33 +185,39 @@ class ClockSampler:
 
 # ---- device-resident steps ------------------------------------------------
 
-def run_device(args, inputs, dtype):
+def run_device(args, inputs, dtype_of, want_state=False):
+    """K steps (after W warm-up steps) of the suite on resident arrays.  Each
+    step is the ten-sweep compute phase of every program from its initial
+    inputs: the working arrays are first restored from device copies of the
+    inputs, then swept with the reference's pointer rotation.  Returns the
+    step time, per-stencil mean sweep time, clocks, kernel launches, whether
+    every value stayed finite, the final means, and (optionally) the final
+    arrays in their roles."""
     import torch
 
     stream = torch.cuda.current_stream()
     sp = kgb200.stream_ptr(stream)
     lib = kgb200.load()
-    probs = {}
-    keep = []
+    seqs, work, pristine = {}, {}, {}
     for name in SUITE:
         coef, arrs, _ = inputs[name]
-        bufs = [torch.from_numpy(a).to("cuda") for a in arrs]
-        keep.append(bufs)
-        probs[name] = [kgb200.problem(name, dtype, shape_of(name), coef[:6], [b.data_ptr() for b in bufs])]
-        # the two-buffer / three-level rotations repeat with period 2 / 3
-        ptrs = [b.data_ptr() for b in bufs]
-        for _ in range(5):
+        pristine[name] = [torch.from_numpy(a).to("cuda") for a in arrs]
+        work[name] = [t.clone() for t in pristine[name]]
+        dt = dtype_of[name]
+        ptrs = [b.data_ptr() for b in work[name]]
+        seq = []
+        for _ in range(NT):
+            seq.append(kgb200.problem(name, dt, shape_of(name), coef[:6], ptrs))
             ptrs = kgb200.rotate(name, ptrs)
-            probs[name].append(kgb200.problem(name, dtype, shape_of(name), coef[:6], ptrs))
+        seqs[name] = seq
     torch.cuda.synchronize()
-
     launches = {"n": 0}
 
     def one_step(events=None):
         for name in SUITE:
-            seq = probs[name]
-            for it in range(NT):
-                p = seq[it % len(seq)] if name not in ("divergence", "gradient") else seq[0]
+            for w, p0 in zip(work[name], pristine[name]):
+                w.copy_(p0, non_blocking=True)
+            for p in seqs[name]:
                 if events is not None:
                     e0 = torch.cuda.Event(enable_timing=True)
                     e1 = torch.cuda.Event(enable_timing=True)
@@ -223,13 +229,6 @@ def run_device(args, inputs, dtype):
                     e1.record(stream)
                     events[name].append((e0, e1))
                 launches["n"] += lib.kg_sweep_launches(p.stencil, p.dtype)
-        # each stencil's sequence continues where the step left it
-        for name in SUITE:
-            if name in ("divergence", "gradient"):
-                continue
-            period = 3 if name == "wave13pt" else 2
-            shift = NT % period
-            probs[name] = probs[name][shift:] + probs[name][:shift]
 
     for _ in range(args.warmup):
         one_step()
@@ -255,10 +254,46 @@ def run_device(args, inputs, dtype):
     for name in SUITE:
         ds = [a.elapsed_time(b) for a, b in events[name]]
         per[name] = sum(ds) / len(ds)
-    finite = all(bool(torch.isfinite(b).all()) for bufs in keep for b in bufs)
-    del keep
-    torch.cuda.empty_cache()
-    return total_ms, per, clk.summary(), launches["n"], finite
+    finite = all(bool(torch.isfinite(b).all()) for name in SUITE for b in work[name])
+    # final roles after NT sweeps and the reference's final means
+    state, means = {}, {}
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for name in SUITE:
+        ptrs = [b.data_ptr() for b in work[name]]
+        for _ in range(NT):
+            ptrs = kgb200.rotate(name, ptrs)
+        by = {b.data_ptr(): b for b in work[name]}
+        roles = [by[q] for q in ptrs]
+        state[name] = roles
+        n = roles[0].numel()
+        if name == "gradient":
+            fin = [roles[1], roles[2], roles[3]]
+        elif name == "divergence":
+            fin = [roles[0]]
+        else:
+            fin = [roles[1]]
+        kgb200.checksum(kgb200.KG_F64, n, [t.data_ptr() for t in fin], out.data_ptr(), stream)
+        means[name] = "final mean = %f" % (float(out.item()) / n / len(fin))
+    del pristine
+    if not want_state:
+        state = None
+    return total_ms, per, clk.summary(), launches["n"], finite, means, state
+
+
+def reference_final_means():
+    """The final-mean lines the reference's gcc binary printed for
+    `benchmark 512 256 256 10` (tests/golden/reference_checksums.json)."""
+    path = os.path.join(ROOT, "tests", "golden", "reference_checksums.json")
+    try:
+        runs = json.load(open(path))["runs"]
+    except Exception:
+        return {}
+    out = {}
+    for name, rs in runs.items():
+        for r in rs:
+            if r.get("readme_config"):
+                out[name] = [ln for ln in r["lines"] if ln.startswith("final mean")][0].rstrip()
+    return out
 
 
 # ---- precision sweep (wave13pt, uxx1; FP64 / FP32 / BF16) ------------------
@@ -281,8 +316,8 @@ def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt"
     lib = kgb200.load()
     stream = torch.cuda.current_stream()
     sp = kgb200.stream_ptr(stream)
-    forms = [("f64", kgb200.KG_F64, torch.float64), ("f32", kgb200.KG_F32, torch.float32),
-             ("bf16", kgb200.KG_BF16, torch.bfloat16)]
+    forms = [("f64", kgb200.KG_F64, torch.float64), ("f64ff", kgb200.KG_F64_FF, torch.float64),
+             ("f32", kgb200.KG_F32, torch.float32), ("bf16", kgb200.KG_BF16, torch.bfloat16)]
     out = {}
     for name in names:
         inputs = make_inputs([name], variant=3, shape=shape)
@@ -291,14 +326,14 @@ def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt"
         del inputs, arrs
         state = {}
         for key, dt, tdt in forms:
-            bufs = f64 if key == "f64" else [t.to(tdt) for t in f64]
+            bufs = f64 if key == "f64" else ([t.clone() for t in f64] if tdt == torch.float64 else [t.to(tdt) for t in f64])
             state[key] = {"dt": dt, "bufs": bufs, "ptrs": [b.data_ptr() for b in bufs], "ms": 0.0,
                           "newest": None}
         out_slot = 2 if name == "wave13pt" else 1
         stats = torch.zeros(4, dtype=torch.float64, device="cuda")
         sums = torch.zeros(1, dtype=torch.float64, device="cuda")
-        errs = {"f32": [], "bf16": []}
-        checks = {"f64": [], "f32": [], "bf16": []}
+        errs = {"f64ff": [], "f32": [], "bf16": []}
+        checks = {"f64": [], "f64ff": [], "f32": [], "bf16": []}
         for block in range(nsteps // every):
             for key, dt, _ in forms:
                 st = state[key]
@@ -661,7 +696,8 @@ def run_reference(args):
 
 METRIC = "Gpts/s, full suite plain FP64 (11 stencils x 10 sweeps, 512x256x256; 2D 512x65536)"
 DATA = "synthetic: the reference main()'s glibc rand() draws, default seed"
-CONFIG = {"workload": "suite-fp64 benchmark 512 256 256 10 (11 stencils x 10 sweeps per step)",
+CONFIG = {"workload": "suite-fp64 benchmark 512 256 256 10 (11 stencils x 10 sweeps per step, "
+                      "each program restarted from its initial inputs by a device copy)",
           "shape_3d": list(SHAPE3), "shape_2d": list(SHAPE2), "sweeps_per_step": 11 * NT,
           "points_per_sweep": NPTS, "l2": "no flush: every array (268 MB) is larger than L2 (129 MB)",
           "parallelism": "replicas"}
@@ -714,8 +750,39 @@ def main():
         return 0
 
     inputs = make_inputs(SUITE)
-    total_ms, per, clocks, launches, finite = run_device(args, inputs, dtype)
-    del inputs
+    dtype_of = {n: dtype for n in SUITE}
+    total_ms, per, clocks, launches, finite, means, state = run_device(
+        args, inputs, dtype_of, want_state=not args.no_forms)
+    ref_means = reference_final_means()
+    checks = {n: {"gpu": means[n], "reference": ref_means.get(n), "match": means[n] == ref_means.get(n)}
+              for n in SUITE if n in ref_means}
+    ff_form = None
+    if not args.no_forms:
+        # the same steps with float-float arithmetic (gameoflife stays strict:
+        # it must be bit-exact), and its error against the strict arrays
+        ff_of = {n: (kgb200.KG_F64 if n == "gameoflife" else kgb200.KG_F64_FF) for n in SUITE}
+        fms, fper, _, _, ffinite, fmeans, fstate = run_device(args, inputs, ff_of, want_state=True)
+        stats = torch.zeros(4, dtype=torch.float64, device="cuda")
+        errs = {}
+        for n in SUITE:
+            worst = 0.0
+            for a, b in zip(fstate[n], state[n]):
+                kgb200.error_stats(kgb200.KG_F64, a.numel(), a.data_ptr(), b.data_ptr(), stats.data_ptr())
+                mx, _, mref, _ = stats.tolist()
+                worst = max(worst, mx / mref if mref else mx)
+            errs[n] = float("%.3g" % worst)
+        ff_form = {
+            "what": "the same suite steps with FP64 storage and float-float arithmetic on the FP32 pipes "
+                    "(KG_F64_FF; gameoflife strict FP64)",
+            "value": round(11 * NT * NPTS * args.steps / (fms * 1e-3) / 1e9, 4), "unit": "Gpts/s",
+            "speedup_vs_strict": round(total_ms / fms, 2),
+            "max_normwise_err_vs_strict_fp64": errs,
+            "ms_per_sweep": {n: round(fper[n], 4) for n in SUITE},
+            "final_means_match_reference": sum(1 for n in SUITE if n in ref_means and fmeans[n] == ref_means[n]),
+            "finite": ffinite}
+        del fstate
+    del inputs, state
+    torch.cuda.empty_cache()
     if args.world > 1:
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -753,6 +820,8 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.dtype, "data": DATA, "config": CONFIG, "roofline": roofline,
         "gpu_launches": launches, "clocks": clocks, "finite": finite, "per_stencil": per_stencil,
+        "final_means_vs_reference": {"matched": sum(1 for c in checks.values() if c["match"]),
+                                     "of": len(checks), "lines": checks},
     }
     if not args.no_e2e:
         dt, h2d, d2h = run_e2e(args, dtype)
@@ -760,7 +829,7 @@ def main():
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "path": "kg_program_run per stencil: cudaMalloc, H2D, 10 sweeps, D2H of the checksum arrays, cudaFree"}
     if not args.no_forms:
-        line["forms"] = {"precision_sweep": dict(
+        line["forms"] = {"fp64_float_float": ff_form, "precision_sweep": dict(
             workload="wave13pt and uxx1, 1024x512x512, 100 steps from a Gaussian pulse (sigma 16) + 1e-3 noise; "
                      "FP64 strict vs FP32 and BF16 storage (FP32 arithmetic); errors relative to FP64 every 10 steps",
             **run_precision())}

@@ -33,7 +33,7 @@ kg_status fail_cuda(cudaError_t e, const char* what)
 size_t dtype_size(int dt)
 {
 	switch (dt) {
-	case KG_F64: case KG_F64_FMA: return 8;
+	case KG_F64: case KG_F64_FMA: case KG_F64_FF: return 8;
 	case KG_F32: return 4;
 	case KG_BF16: case KG_F16: return 2;
 	case KG_U8: return 1;
@@ -62,7 +62,7 @@ static kg_status validate(const kg_problem* p)
 	if (!p) return fail(KG_EINVAL, "null problem");
 	if (p->stencil < 0 || p->stencil >= KG_NSTENCILS) return fail(KG_EINVAL, "unknown stencil %d", p->stencil);
 	const Meta& m = k_meta[p->stencil];
-	if (p->dtype < KG_F64 || p->dtype > KG_U8) return fail(KG_EINVAL, "%s: unknown dtype %d", m.name, p->dtype);
+	if (p->dtype < KG_F64 || p->dtype > KG_F64_FF) return fail(KG_EINVAL, "%s: unknown dtype %d", m.name, p->dtype);
 	if (p->dtype == KG_U8 && p->stencil != KG_GAMEOFLIFE)
 		return fail(KG_ENOTSUP, "%s: byte cells are provided for gameoflife only", m.name);
 	if (p->nx < 0 || p->ny < 0 || p->ns < 0) return fail(KG_EINVAL, "%s: negative size", m.name);
@@ -89,6 +89,7 @@ static cudaError_t dispatch(const kg_problem& p, cudaStream_t st)
 	switch (p.dtype) {
 	case KG_F64: return sweep_f64(p, st);
 	case KG_F64_FMA: return sweep_f64fma(p, st);
+	case KG_F64_FF: return sweep_f64ff(p, st);
 	case KG_F32: return sweep_f32(p, st);
 	case KG_BF16: return sweep_bf16(p, st);
 	case KG_F16: return sweep_f16(p, st);
@@ -246,6 +247,7 @@ kg_status kg_kernel_regcount(int stencil, kg_dtype dt, int* nregs)
 	switch (dt) {
 	case KG_F64: e = regs_f64(p, nregs); break;
 	case KG_F64_FMA: e = regs_f64fma(p, nregs); break;
+	case KG_F64_FF: e = regs_f64ff(p, nregs); break;
 	case KG_F32: e = regs_f32(p, nregs); break;
 	case KG_BF16: e = regs_bf16(p, nregs); break;
 	case KG_F16: e = regs_f16(p, nregs); break;

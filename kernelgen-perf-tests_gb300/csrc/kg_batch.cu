@@ -94,18 +94,18 @@ __global__ void __launch_bounds__(BX * BY) batch_kernel(const BatchDesc* __restr
 		batch_roles<S>(d, step, p);
 		switch (d.stencil) {
 		case KG_LAPLACIAN:
-			sweep_tile<OpLaplacian<N>, N, S, BX, BY, KC>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, p, d.nx, d.ny, d.ns, tx, ty, tz);
+			sweep_tile<OpLaplacian<N>, N, S, BX, BY, KC, 4>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, p, d.nx, d.ny, d.ns, tx, ty, tz);
 			break;
 		case KG_DIVERGENCE:
-			sweep_tile<OpDivergence<N>, N, S, BX, BY, KC>(OpDivergence<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])},
+			sweep_tile<OpDivergence<N>, N, S, BX, BY, KC, 4>(OpDivergence<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])},
 				p, d.nx, d.ny, d.ns, tx, ty, tz);
 			break;
 		case KG_WAVE13PT:
-			sweep_tile<OpWave13pt<N>, N, S, BX, BY, KC>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])},
+			sweep_tile<OpWave13pt<N>, N, S, BX, BY, KC, 4>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])},
 				p, d.nx, d.ny, d.ns, tx, ty, tz);
 			break;
 		case KG_GAUSSBLUR:
-			sweep_tile<OpGaussblur<N>, N, S, BX, BY, KC>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]),
+			sweep_tile<OpGaussblur<N>, N, S, BX, BY, KC, 4>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]),
 				N(d.c[3]), N(d.c[4]), N(d.c[5]), N(d.c[6])}, p, d.nx, d.ny, d.ns, tx, ty, tz);
 			break;
 		default: break;

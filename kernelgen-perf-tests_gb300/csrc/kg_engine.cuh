@@ -26,14 +26,22 @@ template <class N, class S> struct GAcc {
 	__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
 		return Conv<N, S>::ld(in[q] + c + dx + dy * sy + dz * sz);
 	}
+	// The stored value itself, without conversion to N.
+	__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
+		return __ldg(in[q] + c + dx + dy * sy + dz * sz);
+	}
 };
 
 constexpr int kBX = 32, kBY = 8;
 
+
 // One tile: BX x BY columns (threadIdx.x, threadIdx.y) of the update domain,
 // planes [LZ + tz*KC, LZ + (tz+1)*KC).  2D ops (LZ = HZ = 0, ns = 1) walk KC
 // rows instead, BY apart, so a tile covers BX x (BY*KC) points either way.
-template <class Op, class N, class S, int BX, int BY, int KC>
+// The z loop is unrolled UK times so that a thread has the loads of UK
+// planes in flight at once (measured on GB300: FP32 wave13pt 213 -> 348
+// Gpts/s going from 1 to 2).
+template <class Op, class N, class S, int BX, int BY, int KC, int UK = 2>
 __device__ __forceinline__ void sweep_tile(const Op& op, const Ptrs<S>& p, int nx, int ny, int ns,
 	int tx, int ty, int tz)
 {
@@ -59,7 +67,7 @@ __device__ __forceinline__ void sweep_tile(const Op& op, const Ptrs<S>& p, int n
 		const int j = Op::LY + ty * BY + (int)threadIdx.y;
 		if (j >= ny - Op::HY) return;
 		const int k0 = Op::LZ + tz * KC, k1 = min(k0 + KC, ns - Op::HZ);
-#pragma unroll 1
+#pragma unroll UK
 		for (int k = k0; k < k1; k++) {
 			const long long c = i + sy * j + sz * k;
 			GAcc<N, S> at{p.in, c, sy, sz};
@@ -137,27 +145,6 @@ cudaError_t with_op(const kg_problem& pr, F&& f)
 	case KG_GAMEOFLIFE: return f(OpGameoflife<N>{});
 	default: return cudaErrorInvalidValue;
 	}
-}
-
-template <class N, class S>
-cudaError_t sweep_typed(const kg_problem& pr, cudaStream_t st)
-{
-	return with_op<N>(pr, [&](const auto& op) {
-		using Op = std::decay_t<decltype(op)>;
-		return Launch<Op, N, S>::run(op, pr, st);
-	});
-}
-
-template <class N, class S>
-cudaError_t regs_typed(const kg_problem& pr, int* nregs)
-{
-	return with_op<N>(pr, [&](const auto& op) {
-		using Op = std::decay_t<decltype(op)>;
-		cudaFuncAttributes a;
-		cudaError_t e = cudaFuncGetAttributes(&a, Launch<Op, N, S>::func());
-		if (e == cudaSuccess) *nregs = a.numRegs;
-		return e;
-	});
 }
 
 }  // namespace kg

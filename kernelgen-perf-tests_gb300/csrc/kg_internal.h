@@ -11,12 +11,14 @@ namespace kg {
 // translation unit each, compiled in parallel).
 cudaError_t sweep_f64(const kg_problem& p, cudaStream_t s);
 cudaError_t sweep_f64fma(const kg_problem& p, cudaStream_t s);
+cudaError_t sweep_f64ff(const kg_problem& p, cudaStream_t s);
 cudaError_t sweep_f32(const kg_problem& p, cudaStream_t s);
 cudaError_t sweep_bf16(const kg_problem& p, cudaStream_t s);
 cudaError_t sweep_f16(const kg_problem& p, cudaStream_t s);
 cudaError_t sweep_u8(const kg_problem& p, cudaStream_t s);
 cudaError_t regs_f64(const kg_problem& p, int* nregs);
 cudaError_t regs_f64fma(const kg_problem& p, int* nregs);
+cudaError_t regs_f64ff(const kg_problem& p, int* nregs);
 cudaError_t regs_f32(const kg_problem& p, int* nregs);
 cudaError_t regs_bf16(const kg_problem& p, int* nregs);
 cudaError_t regs_f16(const kg_problem& p, int* nregs);

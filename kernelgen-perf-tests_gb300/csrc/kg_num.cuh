@@ -49,6 +49,112 @@ __device__ __forceinline__ FF operator-(FF a, FF b) { return mkf(a.v - b.v); }
 __device__ __forceinline__ FF operator*(FF a, FF b) { return mkf(a.v * b.v); }
 __device__ __forceinline__ FF operator/(FF a, FF b) { return mkf(a.v / b.v); }
 
+// FF2: an FP64 value carried as an unevaluated sum hi + lo of two FP32
+// numbers ("float-float"), computed on the FP32 pipes with error-free
+// transformations: TwoSum (Knuth) for additions, the FMA product error for
+// multiplications.  About 44-48 significant bits survive an operation, so a
+// stencil sweep stays within ~1e-14 of FP64 normwise, while GB300 issues FP32
+// FMAs at 72x its FP64 rate.  Intrinsics (__fadd_rn, __fmul_rn, __fmaf_rn)
+// keep nvcc from re-associating or contracting the compensation terms.
+struct FF2 {
+	float hi, lo;
+	__host__ __device__ constexpr FF2() : hi(0.f), lo(0.f) {}
+	__host__ __device__ constexpr FF2(float h, float l) : hi(h), lo(l) {}
+	// A double constant or coefficient, split once (on the host or folded).
+	__host__ __device__ constexpr explicit FF2(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+};
+__device__ __forceinline__ FF2 ff2_fast_two_sum(float a, float b)
+{
+	const float s = __fadd_rn(a, b);
+	return FF2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ FF2 operator+(FF2 a, FF2 b)
+{
+	const float s = __fadd_rn(a.hi, b.hi);
+	const float bb = __fsub_rn(s, a.hi);
+	const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+	return ff2_fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ FF2 operator-(FF2 b) { return FF2(-b.hi, -b.lo); }
+__device__ __forceinline__ FF2 operator-(FF2 a, FF2 b) { return a + (-b); }
+__device__ __forceinline__ FF2 operator*(FF2 a, FF2 b)
+{
+	const float p = __fmul_rn(a.hi, b.hi);
+	float e = __fmaf_rn(a.hi, b.hi, -p);
+	e = __fmaf_rn(a.hi, b.lo, e);
+	e = __fmaf_rn(a.lo, b.hi, e);
+	return ff2_fast_two_sum(p, e);
+}
+__device__ __forceinline__ FF2 operator/(FF2 a, FF2 b)
+{
+	const float q1 = __fdiv_rn(a.hi, b.hi);
+	const FF2 r = a - b * FF2(q1, 0.f);
+	const float q2 = __fdiv_rn(r.hi, b.hi);
+	return ff2_fast_two_sum(q1, q2);
+}
+
+// FP64 <-> FF2 without the FP64 pipe.  On GB300 the F2F conversions between
+// double and float issue to the FP64 pipe (2 per clock per SM), so both
+// directions are built from the IEEE bit fields with integer and FP32 ops.
+//
+// Split: hi = x truncated to 24 significant bits (exponent rebiased, top 23
+// fraction bits); lo = the 29 remaining fraction bits r, rounded to 24 bits,
+// times 2^(e-1075), with x's sign.  r is converted exactly in two 23-bit
+// pieces with the 2^23 magic-number trick.  |x| below 2^-74 keeps only hi
+// (lo underflows), below 2^-126 becomes a signed zero; inf and nan pass; x
+// above FP32's range becomes inf.
+__device__ __forceinline__ FF2 ff2_from_double(double x)
+{
+	const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+	const unsigned bh = (unsigned)(b >> 32), bl = (unsigned)b;
+	const unsigned sign = bh & 0x80000000u;
+	const int e = (int)((bh >> 20) & 0x7ff);
+	const unsigned fh = ((bh & 0xfffffu) << 3) | (bl >> 29);
+	if (e >= 897 && e <= 1150) {
+		const float hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | fh);
+		float lo = 0.f;
+		if (e >= 949) {
+			const unsigned r = bl & 0x1fffffffu;
+			const float f0 = __fsub_rn(__uint_as_float(0x4b000000u | (r & 0x7fffffu)), 8388608.0f);
+			const float f1 = __fsub_rn(__uint_as_float(0x4b000000u | (r >> 23)), 8388608.0f);
+			const float rf = __fmaf_rn(f1, 8388608.0f, f0);
+			const float scale = __uint_as_float((unsigned)(e - 948) << 23);  // 2^(e - 1075)
+			lo = __uint_as_float(__float_as_uint(__fmul_rn(rf, scale)) | sign);
+		}
+		return FF2(hi, lo);
+	}
+	if (e < 897) return FF2(__uint_as_float(sign), 0.f);
+	const unsigned nan = (e == 0x7ff && ((bh & 0xfffffu) | bl)) ? 0x400000u : 0u;
+	return FF2(__uint_as_float(sign | 0x7f800000u | nan), 0.f);
+}
+
+// Merge: hi's bit fields give its exact FP64 bit pattern; lo, in units of
+// hi's FP64 ulp (an integer below 2^30 for a normalised pair), is added to
+// or subtracted from that pattern.  Below a power-of-two hi the ulp halves,
+// so a subtraction there counts twice.  Bits of lo under hi's FP64 ulp are
+// dropped (error below one FP64 ulp).
+__device__ __forceinline__ double ff2_to_double(FF2 v)
+{
+	const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+	const int eh = (int)((hb >> 23) & 0xff), el = (int)((lb >> 23) & 0xff);
+	const unsigned long long sgn = (unsigned long long)(hb & 0x80000000u) << 32;
+	if (eh == 0) return __longlong_as_double((long long)sgn);  // zero (or FP32-subnormal) hi
+	if (eh == 0xff)
+		return __longlong_as_double((long long)(sgn | 0x7ff0000000000000ULL | ((hb & 0x7fffffu) ? 0x8000000000000ULL : 0)));
+	const unsigned long long dh = sgn | ((unsigned long long)(eh + 896) << 52) | ((unsigned long long)(hb & 0x7fffffu) << 29);
+	if (el == 0) return __longlong_as_double((long long)dh);
+	const int sh = el - eh + 29;
+	const unsigned long long ml = (unsigned long long)((lb & 0x7fffffu) | 0x800000u);
+	unsigned long long l;
+	if (sh >= 0) l = ml << (sh > 34 ? 34 : sh);
+	else if (sh > -25) l = ml >> (-sh);
+	else return __longlong_as_double((long long)dh);
+	const bool same = ((hb ^ lb) & 0x80000000u) == 0;
+	if (same) return __longlong_as_double((long long)(dh + l));
+	if ((hb & 0x7fffffu) == 0) l <<= 1;
+	return __longlong_as_double((long long)(dh - l));
+}
+
 // ---- storage <-> arithmetic -------------------------------------------------
 
 template <class N, class S> struct Conv;
@@ -62,6 +168,11 @@ template <> struct Conv<FD, double> {
 	static __device__ __forceinline__ FD ld(const double* p) { return FD(__ldg(p)); }
 	static __device__ __forceinline__ FD from(double x) { return FD(x); }
 	static __device__ __forceinline__ double to(FD x) { return x.v; }
+};
+template <> struct Conv<FF2, double> {
+	static __device__ __forceinline__ FF2 ld(const double* p) { return ff2_from_double(__ldg(p)); }
+	static __device__ __forceinline__ FF2 from(double x) { return ff2_from_double(x); }
+	static __device__ __forceinline__ double to(FF2 x) { return ff2_to_double(x); }
 };
 template <> struct Conv<FF, float> {
 	static __device__ __forceinline__ FF ld(const float* p) { return mkf(__ldg(p)); }

@@ -6,6 +6,8 @@
 // engine (kg_engine.cuh) supplies the accessor and the iteration.
 #pragma once
 
+#include <type_traits>
+
 #include "kg_num.cuh"
 
 namespace kg {
@@ -18,10 +20,19 @@ struct Slots {
 	int nout;
 };
 
+// Neighbour reach of one input: how far back (x0, y0, z0) and ahead (x1, y1,
+// z1) of the updated point the body reads it.  All zero: read at the point
+// only (the staged engine then reads it from global memory directly).
+struct Halo {
+	int x0, x1, y0, y1, z0, z1;
+	__host__ __device__ constexpr bool center() const { return !(x0 | x1 | y0 | y1 | z0 | z1); }
+};
+
 // laplacian/laplacian.c:81-97
 template <class N> struct OpLaplacian {
 	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 1, HZ = 1;
 	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{1, 1, 1, 1, 1, 1}}; return h[q]; }
 	N alpha, beta;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w0 = 0;
@@ -36,6 +47,7 @@ template <class N> struct OpLaplacian {
 template <class N> struct OpDivergence {
 	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 1, HZ = 1;
 	static constexpr Slots slots() { return {{1, 2, 3}, 3, {0}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{1, 1, 0, 0, 0, 0}, {0, 0, 1, 1, 0, 0}, {0, 0, 0, 0, 1, 1}}; return h[q]; }
 	N alpha, beta, gamma;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int ux = 0, uy = 1, uz = 2;
@@ -49,6 +61,7 @@ template <class N> struct OpDivergence {
 template <class N> struct OpGradient {
 	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 1, HZ = 1;
 	static constexpr Slots slots() { return {{0}, 1, {1, 2, 3}, 3}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{1, 1, 1, 1, 1, 1}}; return h[q]; }
 	N alpha, beta, gamma;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int u = 0;
@@ -63,12 +76,24 @@ template <class N> struct OpGradient {
 template <class N> struct OpUxx1 {
 	static constexpr int LX = 2, HX = 1, LY = 2, HY = 1, LZ = 2, HZ = 1;
 	static constexpr Slots slots() { return {{0, 2, 3, 4, 5}, 5, {1}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{0, 0, 0, 0, 0, 0}, {0, 0, 1, 0, 1, 0}, {2, 1, 0, 0, 0, 0}, {0, 0, 2, 1, 0, 0}, {0, 0, 0, 0, 2, 1}}; return h[q]; }
 	N c1, c2, dth;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int u0 = 0, d1 = 1, xx = 2, xy = 3, xz = 4;
-		N d = N(0.25) * (
-			at(d1, 0, 0, 0) + at(d1, 0, -1, 0) +
-			at(d1, 0, 0, -1) + at(d1, 0, -1, -1));
+		N d;
+		if constexpr (std::is_same<N, FF2>::value) {
+			// The density average can cancel (the reference draws d1 in
+			// [-1,1]); FF2's 2^-48 input rounding would then dominate the
+			// quotient, so it is formed from the FP64 values in FP64 and
+			// rounded to FF2 once, relative to its own size.
+			d = ff2_from_double(0.25 * (
+				at.raw(d1, 0, 0, 0) + at.raw(d1, 0, -1, 0) +
+				at.raw(d1, 0, 0, -1) + at.raw(d1, 0, -1, -1)));
+		} else {
+			d = N(0.25) * (
+				at(d1, 0, 0, 0) + at(d1, 0, -1, 0) +
+				at(d1, 0, 0, -1) + at(d1, 0, -1, -1));
+		}
 		o[0] = at(u0, 0, 0, 0) + (dth / d) * (
 			c1 * (at(xx, 0, 0, 0) - at(xx, -1, 0, 0)) +
 			c2 * (at(xx, 1, 0, 0) - at(xx, -2, 0, 0)) +
@@ -83,6 +108,7 @@ template <class N> struct OpUxx1 {
 template <class N> struct OpWave13pt {
 	static constexpr int LX = 2, HX = 2, LY = 2, HY = 2, LZ = 2, HZ = 2;
 	static constexpr Slots slots() { return {{0, 1}, 2, {2}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{0, 0, 0, 0, 0, 0}, {2, 2, 2, 2, 2, 2}}; return h[q]; }
 	N m0, m1, m2;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w0 = 0, w1 = 1;
@@ -114,6 +140,7 @@ template <class N, bool FROM_ZERO> struct OpTricubicT {
 	static constexpr int LY = FROM_ZERO ? 2 : 1, HY = 2;
 	static constexpr int LZ = FROM_ZERO ? 2 : 1, HZ = 2;
 	static constexpr Slots slots() { return {{0, 2, 3, 4}, 4, {1}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{1, 2, 1, 2, 1, 2}, {0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}}; return h[q]; }
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int u0 = 0, pa = 1, pb = 2, pc = 3;
 		N wa[4], wb[4], wc[4];
@@ -143,6 +170,7 @@ template <class N> using OpTricubic2 = OpTricubicT<N, true>;
 template <class N> struct OpJacobi {
 	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 0, HZ = 0;
 	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{1, 1, 1, 1, 0, 0}}; return h[q]; }
 	N c0, c1, c2;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w0 = 0;
@@ -156,6 +184,7 @@ template <class N> struct OpJacobi {
 template <class N> struct OpLapgsrb {
 	static constexpr int LX = 2, HX = 2, LY = 2, HY = 2, LZ = 2, HZ = 2;
 	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{2, 2, 2, 2, 2, 2}}; return h[q]; }
 	N c0, c1, c2, c3;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w = 0;
@@ -180,6 +209,7 @@ template <class N> struct OpLapgsrb {
 template <class N> struct OpGaussblur {
 	static constexpr int LX = 2, HX = 2, LY = 2, HY = 2, LZ = 0, HZ = 0;
 	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{2, 2, 2, 2, 0, 0}}; return h[q]; }
 	N s0, s1, s2, s4, s5, s8, f;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w = 0;
@@ -198,6 +228,7 @@ template <class N> struct OpGaussblur {
 template <class N> struct OpGameoflife {
 	static constexpr int LX = 1, HX = 1, LY = 1, HY = 1, LZ = 0, HZ = 0;
 	static constexpr Slots slots() { return {{0}, 1, {1}, 1}; }
+	static constexpr Halo halo(int q) { constexpr Halo h[] = {{1, 1, 1, 1, 0, 0}}; return h[q]; }
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int u0 = 0;
 		const N C(100000000000000000000.);

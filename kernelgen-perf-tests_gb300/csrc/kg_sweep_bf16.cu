@@ -1,5 +1,5 @@
 // kg_sweep_bf16.cu -- sweeps with storage __nv_bfloat16, arithmetic FF (kg_num.cuh).
-#include "kg_engine.cuh"
+#include "kg_dispatch.cuh"
 #include "kg_internal.h"
 
 namespace kg {

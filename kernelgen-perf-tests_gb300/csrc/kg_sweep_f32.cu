@@ -1,5 +1,5 @@
 // kg_sweep_f32.cu -- sweeps with storage float, arithmetic FF (kg_num.cuh).
-#include "kg_engine.cuh"
+#include "kg_dispatch.cuh"
 #include "kg_internal.h"
 
 namespace kg {

@@ -1,5 +1,5 @@
 // kg_sweep_f64fma.cu -- sweeps with storage double, arithmetic FD (kg_num.cuh).
-#include "kg_engine.cuh"
+#include "kg_dispatch.cuh"
 #include "kg_internal.h"
 
 namespace kg {

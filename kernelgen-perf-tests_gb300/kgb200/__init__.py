@@ -10,7 +10,9 @@ import subprocess
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REPO_DIR = os.path.dirname(PKG_DIR)
-LIB_PATH = os.path.join(PKG_DIR, "build", "libkg_b200.so")
+# KG_B200_LIB selects another build of the same library (e.g. one compiled
+# with different engine options); the default is the in-tree build.
+LIB_PATH = os.environ.get("KG_B200_LIB") or os.path.join(PKG_DIR, "build", "libkg_b200.so")
 HEADER = os.path.join(REPO_DIR, "include", "kg_b200.h")
 
 STENCILS = ["laplacian", "divergence", "gradient", "uxx1", "wave13pt", "tricubic",
@@ -18,10 +20,10 @@ STENCILS = ["laplacian", "divergence", "gradient", "uxx1", "wave13pt", "tricubic
 STENCIL_ID = {s: i for i, s in enumerate(STENCILS)}
 IS2D = {"jacobi", "gaussblur", "gameoflife"}
 
-KG_F64, KG_F64_FMA, KG_F32, KG_BF16, KG_F16, KG_U8 = range(6)
+KG_F64, KG_F64_FMA, KG_F32, KG_BF16, KG_F16, KG_U8, KG_F64_FF = range(7)
 DTYPES = {"f64": KG_F64, "f64fma": KG_F64_FMA, "f32": KG_F32, "bf16": KG_BF16,
-          "f16": KG_F16, "u8": KG_U8}
-DTYPE_SIZE = {KG_F64: 8, KG_F64_FMA: 8, KG_F32: 4, KG_BF16: 2, KG_F16: 2, KG_U8: 1}
+          "f16": KG_F16, "u8": KG_U8, "f64ff": KG_F64_FF}
+DTYPE_SIZE = {KG_F64: 8, KG_F64_FMA: 8, KG_F32: 4, KG_BF16: 2, KG_F16: 2, KG_U8: 1, KG_F64_FF: 8}
 STATUS = ["KG_OK", "KG_EINVAL", "KG_ECUDA", "KG_ENOMEM", "KG_ETIMEOUT", "KG_ENOTSUP", "KG_ENODEV"]
 
 # Every extern "C" symbol the header declares (checked by the CPU tests).
