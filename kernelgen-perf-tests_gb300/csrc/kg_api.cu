@@ -1,6 +1,8 @@
 // kg_api.cu -- the C ABI: argument checks, dispatch by storage type, errors.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "kg_internal.h"

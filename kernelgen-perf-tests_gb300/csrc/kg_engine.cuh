@@ -10,6 +10,9 @@
 
 #include <cuda_runtime.h>
 
+#include <cstring>
+#include <type_traits>
+
 #include "../../include/kg_b200.h"
 #include "kg_ops.cuh"
 

@@ -27,6 +27,98 @@ __device__ __forceinline__ SD operator-(SD a, SD b) { return SD(__dsub_rn(a.v, b
 __device__ __forceinline__ SD operator*(SD a, SD b) { return SD(__dmul_rn(a.v, b.v)); }
 __device__ __forceinline__ SD operator/(SD a, SD b) { return SD(__ddiv_rn(a.v, b.v)); }
 
+// SE: the same strict FP64 semantics as SD, computed on the integer pipes.
+// Additions, subtractions and multiplications are exact IEEE round-to-
+// nearest-even operations built from 32-bit integer arithmetic (53-bit
+// mantissas in two words, 106-bit products from four 32x32 multiplies,
+// guard/round/sticky rounding), so their bits equal the FP64 unit's.  Zeros,
+// subnormals, infinities, NaNs and results leaving the normal range take a
+// rarely used branch to the FP64 unit; division always does.  GB300 issues
+// FP64 arithmetic at 1/72 of its FP32 rate while the integer pipes sit idle
+// in these sweeps: measured, a thread that interleaves independent native
+// and integer multiplies reaches 1.9x the FP64 unit's multiply rate, bit for
+// bit the same (strict tricubic uses this).  Whole warps computing in SE
+// beside warps in SD were slower: the stencils' sums are dependent chains.
+struct SE {
+	double v;
+	__host__ __device__ constexpr SE() : v(0) {}
+	__host__ __device__ constexpr explicit SE(double x) : v(x) {}
+};
+
+static __device__ __noinline__ double se_native_mul(double a, double b) { return __dmul_rn(a, b); }
+static __device__ __noinline__ double se_native_add(double a, double b) { return __dadd_rn(a, b); }
+
+__device__ __forceinline__ double se_mul(double a, double b)
+{
+	const unsigned long long A = (unsigned long long)__double_as_longlong(a);
+	const unsigned long long B = (unsigned long long)__double_as_longlong(b);
+	const unsigned ahw = (unsigned)(A >> 32), bhw = (unsigned)(B >> 32);
+	const int ea = (ahw >> 20) & 0x7ff, eb = (bhw >> 20) & 0x7ff;
+	const unsigned ah = (ahw & 0xfffffu) | 0x100000u, bh = (bhw & 0xfffffu) | 0x100000u;
+	const unsigned al = (unsigned)A, bl = (unsigned)B;
+	// 53 x 53 -> 106-bit product P = ah bh 2^64 + (ah bl + al bh) 2^32 + al bl
+	const unsigned long long p0 = (unsigned long long)al * bl;
+	const unsigned long long p1 = (unsigned long long)ah * bl;
+	const unsigned long long p2 = (unsigned long long)al * bh;
+	const unsigned long long p3 = (unsigned long long)ah * bh;
+	const unsigned long long mid = p1 + p2 + (p0 >> 32);
+	const unsigned long long hi = (p3 << 22) + (mid >> 10);          // P >> 42, in [2^62, 2^64)
+	const bool low_nz = ((unsigned)(mid & 0x3ffu) | (unsigned)p0) != 0;
+	const int top = (int)(hi >> 63);                                 // P >= 2^105
+	const int sh = 10 + top;
+	unsigned long long mant = hi >> sh;                              // 53 bits
+	const unsigned long long rnd = (hi >> (sh - 1)) & 1;
+	const bool stk = low_nz || (hi & ((1ull << (sh - 1)) - 1)) != 0;
+	mant += rnd & ((unsigned long long)stk | (mant & 1));
+	const int E = ea + eb - 1023 + top;
+	const bool ok = (unsigned)(ea - 1) < 2046u && (unsigned)(eb - 1) < 2046u && E >= 1 && E <= 2045;
+	if (__builtin_expect(!ok, 0)) return se_native_mul(a, b);
+	const unsigned long long sign = (A ^ B) & 0x8000000000000000ull;
+	return __longlong_as_double((long long)(sign | (((unsigned long long)(E - 1) << 52) + mant)));
+}
+
+__device__ __forceinline__ double se_add(double a, double b)
+{
+	unsigned long long A = (unsigned long long)__double_as_longlong(a);
+	unsigned long long B = (unsigned long long)__double_as_longlong(b);
+	if ((A & 0x7fffffffffffffffull) < (B & 0x7fffffffffffffffull)) { const unsigned long long t = A; A = B; B = t; }
+	const int ea = (int)((A >> 52) & 0x7ff), eb = (int)((B >> 52) & 0x7ff);
+	bool ok = (unsigned)(ea - 1) < 2046u && (unsigned)(eb - 1) < 2046u;
+	if (__builtin_expect(!ok, 0)) return se_native_add(a, b);
+	const int dd = ea - eb;                                          // |a| >= |b|
+	if (dd > 54) return __longlong_as_double((long long)A);          // b below a quarter ulp of a
+	const unsigned long long Ma = ((A & 0xfffffffffffffull) | 0x10000000000000ull) << 10;
+	const unsigned long long Mb0 = ((B & 0xfffffffffffffull) | 0x10000000000000ull) << 10;
+	const unsigned long long Mb = Mb0 >> dd;
+	const unsigned long long stk_in = dd == 0 ? 0ull : (unsigned long long)((Mb0 << (64 - dd)) != 0);
+	unsigned long long S, stk = stk_in;
+	int E = ea;
+	if (((A ^ B) >> 63) == 0) {
+		S = Ma + Mb;
+		if (S >> 63) { stk |= S & 1; S >>= 1; E += 1; }
+	} else {
+		S = Ma - Mb - stk_in;                                        // truncated b: true S lies in (S-1, S]
+		if (S == 0 && !stk_in) return 0.0;                           // exact cancellation: +0
+		const int lz = __clzll((long long)S) - 1;
+		S <<= lz;
+		E -= lz;
+	}
+	const unsigned long long mant0 = S >> 10;
+	const unsigned long long rnd = (S >> 9) & 1;
+	stk |= (unsigned long long)((S & 0x1ff) != 0);
+	const unsigned long long mant = mant0 + (rnd & (stk | (mant0 & 1)));
+	if (__builtin_expect(E < 1 || E > 2045, 0)) return se_native_add(a, b);
+	return __longlong_as_double((long long)((A & 0x8000000000000000ull) | (((unsigned long long)(E - 1) << 52) + mant)));
+}
+
+__device__ __forceinline__ SE operator+(SE a, SE b) { return SE(se_add(a.v, b.v)); }
+__device__ __forceinline__ SE operator-(SE a, SE b)
+{
+	return SE(se_add(a.v, __longlong_as_double(__double_as_longlong(b.v) ^ (long long)0x8000000000000000ull)));
+}
+__device__ __forceinline__ SE operator*(SE a, SE b) { return SE(se_mul(a.v, b.v)); }
+__device__ __forceinline__ SE operator/(SE a, SE b) { return SE(__ddiv_rn(a.v, b.v)); }
+
 struct FD {
 	double v;
 	__host__ __device__ constexpr FD() : v(0) {}
@@ -163,6 +255,11 @@ template <> struct Conv<SD, double> {
 	static __device__ __forceinline__ SD ld(const double* p) { return SD(__ldg(p)); }
 	static __device__ __forceinline__ SD from(double x) { return SD(x); }
 	static __device__ __forceinline__ double to(SD x) { return x.v; }
+};
+template <> struct Conv<SE, double> {
+	static __device__ __forceinline__ SE ld(const double* p) { return SE(__ldg(p)); }
+	static __device__ __forceinline__ SE from(double x) { return SE(x); }
+	static __device__ __forceinline__ double to(SE x) { return x.v; }
 };
 template <> struct Conv<FD, double> {
 	static __device__ __forceinline__ FD ld(const double* p) { return FD(__ldg(p)); }

@@ -133,6 +133,15 @@ template <class N> __device__ __forceinline__ void tricubic_weights(N a, N* w) {
 	w[3] = N(-1.0 / 6.0) * (a - one) * a * (a + one);
 }
 
+// Strict FP64 tricubic: of the four x-neighbours ii of every (jj, kk) row,
+// the first kTricubicEmu have their *wc and *u0 products formed by the
+// exact integer multiply (se_mul).  Measured on GB300 (512x256x256, ms per
+// sweep): all on the FP64 unit 15.85; 1 of 4 13.65; 2 of 4 12.22; 3 of 4
+// 11.9; 4 of 4 25.6.  Moving part of the in-order sum, the weight
+// polynomials or the wa*wb products as well was slower (those are
+// dependent chains, and the integer operations' latency then shows).
+constexpr int kTricubicEmu = 3;
+
 // tricubic/tricubic.c:1062-1145 (64 terms, t0 + t1 + ... + t63, x fastest)
 // and tricubic2/tricubic2.c:98-102 (u1 = 0; u1 += t_n, same term order).
 template <class N, bool FROM_ZERO> struct OpTricubicT {
@@ -147,6 +156,37 @@ template <class N, bool FROM_ZERO> struct OpTricubicT {
 		tricubic_weights(at(pa, 0, 0, 0), wa);
 		tricubic_weights(at(pb, 0, 0, 0), wb);
 		tricubic_weights(at(pc, 0, 0, 0), wc);
+		if constexpr (std::is_same<N, SD>::value) {
+			// Strict FP64: the same products and sum, but a share of the 128
+			// products (wa*wb)*wc and (...)*u0 is formed by the exact integer
+			// multiply of SE (bitwise equal to the FP64 unit's).  The 64 terms
+			// are independent, so each thread keeps both the FP64 pipe and the
+			// integer pipes busy; the sum stays on the FP64 pipe, in order.
+			double wab[16];
+#pragma unroll
+			for (int jj = 0; jj < 4; jj++)
+#pragma unroll
+				for (int ii = 0; ii < 4; ii++)
+					wab[jj * 4 + ii] = __dmul_rn(wa[ii].v, wb[jj].v);
+			double s = 0.0;
+#pragma unroll
+			for (int kk = 0; kk < 4; kk++)
+#pragma unroll
+				for (int jj = 0; jj < 4; jj++)
+#pragma unroll
+					for (int ii = 0; ii < 4; ii++) {
+						const double u = at(u0, ii - 1, jj - 1, kk - 1).v;
+						const double w = wab[jj * 4 + ii];
+						const double pw = ii < kTricubicEmu ? se_mul(w, wc[kk].v) : __dmul_rn(w, wc[kk].v);
+						const double t = ii < kTricubicEmu ? se_mul(pw, u) : __dmul_rn(pw, u);
+						if (kk == 0 && jj == 0 && ii == 0)
+							s = FROM_ZERO ? __dadd_rn(0.0, t) : t;
+						else
+							s = __dadd_rn(s, t);
+					}
+			o[0] = N(s);
+			return;
+		}
 		N s;
 #pragma unroll
 		for (int kk = 0; kk < 4; kk++)

@@ -322,3 +322,5 @@ def test_b200_driver_gameoflife_bernoulli_u8():
     live = float(np.mean(case.arrays()[1] > 0.5))
     out = driver_lines("gameoflife", [128, 512, 10], {"B200_PREC": "u8", "B200_INIT": "bernoulli"})
     assert "final mean = %f" % live in out
+
+
