@@ -121,11 +121,26 @@ kg_status kg_gameoflife(kg_dtype dt, int nx, int ny,
 
 /* ---- table-driven form of the same entry points ------------------------ */
 
+/* Which kernel design runs a sweep (kg_problem.engine).  AUTO: TMA for
+ * KG_F32/KG_BF16/KG_F16 laplacian, divergence, gradient, uxx1 and lapgsrb
+ * where every array and row starts on a 16-byte boundary, else DIRECT;
+ * DIRECT for KG_F64/KG_F64_FMA; STAGED for KG_F64_FF.  Built: DIRECT and TMA
+ * for every floating type but KG_F64_FF; STAGED and TMA for KG_F64_FF; DIRECT
+ * for KG_U8.  The engines evaluate the same expressions in the same order (the
+ * tests check their outputs equal bit for bit).  TMA needs 16-byte aligned
+ * arrays and rows. */
+typedef enum {
+	KG_ENGINE_AUTO = 0,
+	KG_ENGINE_DIRECT = 1,   /* one thread per column, neighbours through L1     */
+	KG_ENGINE_STAGED = 2,   /* halo planes in shared memory, loaded by threads  */
+	KG_ENGINE_TMA = 3       /* halo planes in shared memory by tiled bulk copy  */
+} kg_engine;
+
 typedef struct {
 	int32_t stencil;     /* kg_stencil */
 	int32_t dtype;       /* kg_dtype   */
 	int32_t nx, ny, ns;  /* 2D stencils: ns = 1 */
-	int32_t reserved;
+	int32_t engine;      /* kg_engine (0 = AUTO) */
 	double coef[6];      /* coefficients in the reference's argument order */
 	void* arr[6];        /* arrays in the reference's argument order       */
 } kg_problem;
@@ -138,6 +153,11 @@ int kg_stencil_outputs(int stencil);
 
 /* One sweep of p (device pointers). */
 kg_status kg_sweep(const kg_problem* p, kg_stream_t stream);
+
+/* Waits for `stream`, then reports whether a TMA-engine sweep since the last
+ * call gave up waiting for its tile copies (KG_ETIMEOUT: that sweep's output
+ * is incomplete) and clears the record.  No counterpart in the reference. */
+kg_status kg_engine_status(kg_stream_t stream);
 
 /* ---- checksums (the reference's "initial mean" / "final mean") ---------- */
 
@@ -180,7 +200,8 @@ kg_status kg_convert(kg_dtype dst_t, void* dst, kg_dtype src_t, const void* src,
 /* ---- whole test program on host arrays ---------------------------------- */
 
 typedef struct {
-	double alloc, load, compute, save, free_;  /* seconds, host wall clock   */
+	double alloc;           /* seconds on the host clock to enqueue allocs  */
+	double load, compute, save, free_;  /* seconds, CUDA events on stream  */
 	double kernel_avg;      /* mean device time of one sweep (CUDA events)  */
 	double kernel_min;
 	int nregs;              /* registers per thread of the sweep kernel     */
@@ -193,7 +214,12 @@ typedef struct {
  * three-level rotation; divergence and gradient no swap), copy back the
  * arrays selected by copy_back_mask (bit q = p->arr[q] in its final role),
  * free.  On return p->arr holds the host arrays in their final roles, as the
- * reference's idxs[] leaves them.  timings may be NULL. */
+ * reference's idxs[] leaves them.  timings may be NULL.
+ * Every phase is ordered on `stream` (device memory from a library-owned
+ * stream-ordered pool that keeps up to 8 GiB cached between calls) and the
+ * call waits for the stream once, at the end; so calls from different host
+ * threads on different streams overlap one program's copies with another's
+ * sweeps.  The host arrays should be pinned for the copies to overlap. */
 kg_status kg_program_run(kg_problem* p, int nt, int copy_back_mask, kg_timings* timings,
 	kg_stream_t stream);
 

@@ -1,46 +1,104 @@
 // kg_dispatch.cuh -- which engine runs a sweep of a given arithmetic.
 //
-// Strict and contracted FP64 (SD, FD) are bound by the FP64 pipe and FP32
-// (FF) by memory; they use the direct engine (kg_engine.cuh), whose neighbour
-// loads hit L1.  Float-float arithmetic (FF2) is bound by issue slots; it uses
-// the staged engine (kg_staged.cuh), which moves each value into shared
-// memory once and splits it into its pair once instead of once per use.
+// Engines (kg_problem.engine, KG_ENGINE_AUTO picks per arithmetic):
+//   direct (kg_engine.cuh)  one thread per (i, j) column, neighbours through L1;
+//   staged (kg_staged.cuh)  halo planes in shared memory, loaded by all threads
+//                           and converted once to the arithmetic's pair;
+//   tma    (kg_tma.cuh)     halo planes in shared memory, moved by tiled bulk
+//                           copies, own column in registers.
+// Strict and contracted FP64 (SD, FD) are bound by the FP64 pipe and run
+// direct by default; FP32 arithmetic (FF) is bound by memory and runs on the
+// TMA engine for the stencils where that measured faster on GB300 (FP32,
+// 512x256x256 and 1024x512x512, Gpts/s direct -> TMA: laplacian 443 -> 493,
+// divergence 343 -> 382, gradient 238 -> 328, uxx1 170 -> 213, lapgsrb 260 ->
+// 268, BF16 uxx1 162 -> 245), where the arrays allow it, and direct for the
+// rest (wave13pt 341 vs 277, tricubic 95 vs 93, the 2D stencils);
+// float-float (FF2) is bound by issue slots and runs staged, which splits each
+// value once instead of once per use.
 #pragma once
 
 #include <type_traits>
 
 #include "kg_engine.cuh"
 #include "kg_staged.cuh"
+#include "kg_tma.cuh"
 
 namespace kg {
 
-// KG_FF_STAGED=1 at build time moves FP32 arithmetic to the staged engine too.
+// KG_FF_STAGED=1 at build time compiles the staged engine for FP32 too.
 #ifndef KG_FF_STAGED
 #define KG_FF_STAGED 0
 #endif
+
+template <class N> struct Engines {
+	static constexpr bool ff2 = std::is_same<N, FF2>::value;
+	static constexpr bool ff = std::is_same<N, FF>::value;
+	static constexpr bool direct = !ff2;
+	static constexpr bool staged = ff2 || (ff && KG_FF_STAGED);
+	static constexpr bool tma = true;
+	static constexpr int automatic = ff2 ? KG_ENGINE_STAGED : ff ? KG_ENGINE_TMA : KG_ENGINE_DIRECT;
+};
+
+inline bool tma_preferred(int stencil)
+{
+	return stencil == KG_LAPLACIAN || stencil == KG_DIVERGENCE || stencil == KG_GRADIENT ||
+		stencil == KG_UXX1 || stencil == KG_LAPGSRB;
+}
+
+template <class N> int automatic_engine(int stencil)
+{
+	const int e = Engines<N>::automatic;
+	return e == KG_ENGINE_TMA && !tma_preferred(stencil) ? KG_ENGINE_DIRECT : e;
+}
+
 template <class Op, class N, class S>
-using LaunchFor = typename std::conditional<std::is_same<N, FF2>::value || (KG_FF_STAGED && std::is_same<N, FF>::value),
-	StagedLaunch<Op, N, S>, Launch<Op, N, S>>::type;
+int resolve_engine(const kg_problem& pr)
+{
+	if (pr.engine != KG_ENGINE_AUTO) return pr.engine;
+	const int e = automatic_engine<N>(pr.stencil);
+	if (e == KG_ENGINE_TMA && !TmaLaunch<Op, N, S>::usable(pr)) return KG_ENGINE_DIRECT;
+	return e;
+}
 
 template <class N, class S>
 cudaError_t sweep_typed(const kg_problem& pr, cudaStream_t st)
 {
-	return with_op<N>(pr, [&](const auto& op) {
+	return with_op<N>(pr, [&](const auto& op) -> cudaError_t {
 		using Op = std::decay_t<decltype(op)>;
-		return LaunchFor<Op, N, S>::run(op, pr, st);
+		const int e = resolve_engine<Op, N, S>(pr);
+		if constexpr (Engines<N>::tma)
+			if (e == KG_ENGINE_TMA)
+				return TmaLaunch<Op, N, S>::usable(pr) ? TmaLaunch<Op, N, S>::run(op, pr, st) : cudaErrorInvalidValue;
+		if constexpr (Engines<N>::staged)
+			if (e == KG_ENGINE_STAGED) return StagedLaunch<Op, N, S>::run(op, pr, st);
+		if constexpr (Engines<N>::direct)
+			if (e == KG_ENGINE_DIRECT) return Launch<Op, N, S>::run(op, pr, st);
+		return cudaErrorNotSupported;
 	});
 }
 
+// Registers per thread of the kernel the automatic choice runs on aligned arrays.
 template <class N, class S>
 cudaError_t regs_typed(const kg_problem& pr, int* nregs)
 {
-	return with_op<N>(pr, [&](const auto& op) {
+	return with_op<N>(pr, [&](const auto& op) -> cudaError_t {
 		using Op = std::decay_t<decltype(op)>;
+		const void* f = nullptr;
+		const int e = automatic_engine<N>(pr.stencil);
+		if constexpr (Engines<N>::tma)
+			if (e == KG_ENGINE_TMA) f = TmaLaunch<Op, N, S>::func();
+		if constexpr (Engines<N>::staged)
+			if (e == KG_ENGINE_STAGED) f = StagedLaunch<Op, N, S>::func();
+		if constexpr (Engines<N>::direct)
+			if (e == KG_ENGINE_DIRECT) f = Launch<Op, N, S>::func();
 		cudaFuncAttributes a;
-		cudaError_t e = cudaFuncGetAttributes(&a, LaunchFor<Op, N, S>::func());
-		if (e == cudaSuccess) *nregs = a.numRegs;
-		return e;
+		cudaError_t err = cudaFuncGetAttributes(&a, f);
+		if (err == cudaSuccess) *nregs = a.numRegs;
+		return err;
 	});
 }
+
+// Engines built for a storage type (bit e set: engine e available).
+constexpr int engines_mask_ff() { return (1 << KG_ENGINE_DIRECT) | (1 << KG_ENGINE_TMA) | (KG_FF_STAGED ? 1 << KG_ENGINE_STAGED : 0); }
 
 }  // namespace kg

@@ -1,7 +1,9 @@
 // kg_runtime.cu -- whole test programs on host arrays, and CUDA-graph plans
 // of the nt-sweep time loop.
 #include <chrono>
+#include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "kg_internal.h"
@@ -29,6 +31,41 @@ static double now_s()
 	return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+
+// Device memory of kg_program_run: one stream-ordered pool per device, owned
+// by the library.  Allocating and freeing on the stream keeps programs that
+// run concurrently on different streams from waiting on each other (cudaFree
+// waits for the whole device); up to kPoolKeep bytes stay cached between
+// calls, the rest goes back to the device when a stream synchronises.
+constexpr uint64_t kPoolKeep = 8ull << 30;
+
+static cudaError_t program_pool(cudaMemPool_t* out)
+{
+	static std::mutex m;
+	static cudaMemPool_t pools[64];
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+	std::lock_guard<std::mutex> g(m);
+	if (!pools[dev]) {
+		cudaMemPoolProps props;
+		memset(&props, 0, sizeof(props));
+		props.allocType = cudaMemAllocationTypePinned;
+		props.location.type = cudaMemLocationTypeDevice;
+		props.location.id = dev;
+		cudaMemPool_t pool;
+		if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
+		uint64_t keep = kPoolKeep;
+		if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
+			cudaMemPoolDestroy(pool);
+			return e;
+		}
+		pools[dev] = pool;
+	}
+	*out = pools[dev];
+	return cudaSuccess;
+}
 }  // namespace kg
 
 using namespace kg;
@@ -59,71 +96,83 @@ kg_status kg_program_run(kg_problem* p, int nt, int copy_back_mask, kg_timings* 
 	cudaStream_t st = (cudaStream_t)stream;
 	kg_timings t;
 	memset(&t, 0, sizeof(t));
+	cudaMemPool_t pool;
+	kg_status s = fail_cuda(program_pool(&pool), "kg_program_run: memory pool");
+	if (s != KG_OK) return s;
+
+	// Every phase is ordered on the stream and the host waits once, at the
+	// end; phase times come from events between the phases.
+	const int nev = 2 * nt + 6;
+	cudaEvent_t* ev = new (std::nothrow) cudaEvent_t[nev];
+	if (!ev) return fail(KG_ENOMEM, "kg_program_run: events");
+	int made = 0;
+	for (; made < nev; made++)
+		if ((s = fail_cuda(cudaEventCreate(&ev[made]), "kg_program_run: events")) != KG_OK) break;
+	cudaEvent_t *load0 = ev, *load1 = ev + 1, *save0 = ev + 2, *save1 = ev + 3, *free1 = ev + 4,
+		*sweep = ev + 6;
 
 	void* dev[6] = {0};
 	kg_problem d = *p;
-	kg_status s = KG_OK;
-	cudaEvent_t* ev = nullptr;
-
-	double t0 = now_s();
-	for (int q = 0; q < narr; q++) {
-		cudaError_t e = cudaMalloc(&dev[q], bytes ? bytes : 1);
-		if (e != cudaSuccess) { s = fail_cuda(e, "kg_program_run: cudaMalloc"); goto out; }
-		d.arr[q] = dev[q];
+	int ran = 0;
+	if (s == KG_OK) {
+		const double t0 = now_s();
+		for (int q = 0; q < narr && s == KG_OK; q++) {
+			s = fail_cuda(cudaMallocFromPoolAsync(&dev[q], bytes ? bytes : 1, pool, st), "kg_program_run: alloc");
+			d.arr[q] = dev[q];
+		}
+		t.alloc = now_s() - t0;
 	}
-	t.alloc = now_s() - t0;
-
-	t0 = now_s();
-	for (int q = 0; q < narr; q++) {
-		cudaError_t e = cudaMemcpyAsync(dev[q], p->arr[q], bytes, cudaMemcpyHostToDevice, st);
-		if (e != cudaSuccess) { s = fail_cuda(e, "kg_program_run: load"); goto out; }
+	if (s == KG_OK) {
+		cudaEventRecord(*load0, st);
+		for (int q = 0; q < narr && s == KG_OK; q++)
+			s = fail_cuda(cudaMemcpyAsync(dev[q], p->arr[q], bytes, cudaMemcpyHostToDevice, st), "kg_program_run: load");
+		cudaEventRecord(*load1, st);
 	}
-	if ((s = fail_cuda(cudaStreamSynchronize(st), "kg_program_run: load")) != KG_OK) goto out;
-	t.load = now_s() - t0;
-
-	ev = new (std::nothrow) cudaEvent_t[2 * (size_t)nt + 2];
-	if (!ev) { s = fail(KG_ENOMEM, "kg_program_run: events"); goto out; }
-	for (int i = 0; i < 2 * nt; i++) cudaEventCreate(&ev[i]);
-	t0 = now_s();
-	for (int it = 0; it < nt; it++) {
-		cudaEventRecord(ev[2 * it], st);
+	for (int it = 0; it < nt && s == KG_OK; it++) {
+		cudaEventRecord(sweep[2 * it], st);
 		if ((s = sweep_checked(&d, st)) != KG_OK) break;
-		cudaEventRecord(ev[2 * it + 1], st);
+		cudaEventRecord(sweep[2 * it + 1], st);
 		rotate_roles(p->stencil, d.arr);
 		rotate_roles(p->stencil, p->arr);
+		ran++;
 	}
-	if (s == KG_OK) s = fail_cuda(cudaStreamSynchronize(st), "kg_program_run: compute");
-	t.compute = now_s() - t0;
-	if (s == KG_OK && nt > 0) {
+	if (s == KG_OK) {
+		cudaEventRecord(*save0, st);
+		for (int q = 0; q < narr && s == KG_OK; q++) {
+			if (!((copy_back_mask >> q) & 1)) continue;
+			s = fail_cuda(cudaMemcpyAsync(p->arr[q], d.arr[q], bytes, cudaMemcpyDeviceToHost, st), "kg_program_run: save");
+		}
+		cudaEventRecord(*save1, st);
+	}
+	for (int q = 0; q < narr; q++)
+		if (dev[q]) cudaFreeAsync(dev[q], st);
+	if (made == nev) cudaEventRecord(*free1, st);
+	const kg_status sync = fail_cuda(cudaStreamSynchronize(st), "kg_program_run");
+	if (s == KG_OK) s = sync;
+	if (s == KG_OK) {
+		float ms = 0;
+		cudaEventElapsedTime(&ms, *load0, *load1);
+		t.load = ms * 1e-3;
+		cudaEventElapsedTime(&ms, *load1, *save0);
+		t.compute = ms * 1e-3;
+		cudaEventElapsedTime(&ms, *save0, *save1);
+		t.save = ms * 1e-3;
+		cudaEventElapsedTime(&ms, *save1, *free1);
+		t.free_ = ms * 1e-3;
 		double sum = 0, mn = 1e30;
-		for (int it = 0; it < nt; it++) {
-			float ms = 0;
-			cudaEventElapsedTime(&ms, ev[2 * it], ev[2 * it + 1]);
+		for (int it = 0; it < ran; it++) {
+			cudaEventElapsedTime(&ms, sweep[2 * it], sweep[2 * it + 1]);
 			sum += ms * 1e-3;
 			if (ms * 1e-3 < mn) mn = ms * 1e-3;
 		}
-		t.kernel_avg = sum / nt;
-		t.kernel_min = mn;
+		if (ran) {
+			t.kernel_avg = sum / ran;
+			t.kernel_min = mn;
+		}
+		kg_kernel_regcount(p->stencil, (kg_dtype)p->dtype, &t.nregs);
 	}
-	for (int i = 0; i < 2 * nt; i++) cudaEventDestroy(ev[i]);
+	for (int i = 0; i < made; i++) cudaEventDestroy(ev[i]);
 	delete[] ev;
-	if (s != KG_OK) goto out;
-	kg_kernel_regcount(p->stencil, (kg_dtype)p->dtype, &t.nregs);
-
-	t0 = now_s();
-	for (int q = 0; q < narr; q++) {
-		if (!((copy_back_mask >> q) & 1)) continue;
-		cudaError_t e = cudaMemcpyAsync(p->arr[q], d.arr[q], bytes, cudaMemcpyDeviceToHost, st);
-		if (e != cudaSuccess) { s = fail_cuda(e, "kg_program_run: save"); goto out; }
-	}
-	if ((s = fail_cuda(cudaStreamSynchronize(st), "kg_program_run: save")) != KG_OK) goto out;
-	t.save = now_s() - t0;
-
-out:
-	t0 = now_s();
-	for (int q = 0; q < narr; q++)
-		if (dev[q]) cudaFree(dev[q]);
-	t.free_ = now_s() - t0;
 	if (tm) *tm = t;
 	return s;
 }

@@ -13,6 +13,7 @@
  *   B200_INIT  reference (default) | bernoulli | unit | pulse
  *   B200_MODE  plain (default: one launch per sweep, timed) | graph (the
  *              nt-sweep loop replayed as one CUDA graph)
+ *   B200_ENGINE auto (default) | direct | staged | tma (kg_problem.engine)
  *   NO_TIMING, PROFILING_FNAME as in the reference.
  * With PROFILING_FNAME set it prints "<name> regcount = N" and, per sweep,
  * "<name> kernel time = t" (device time from CUDA events), the two lines the
@@ -72,6 +73,16 @@ static kg_dtype parse_prec(const char* s)
 	exit(1);
 }
 
+static int parse_engine(const char* s)
+{
+	if (!s || !*s || !strcmp(s, "auto")) return KG_ENGINE_AUTO;
+	if (!strcmp(s, "direct")) return KG_ENGINE_DIRECT;
+	if (!strcmp(s, "staged")) return KG_ENGINE_STAGED;
+	if (!strcmp(s, "tma")) return KG_ENGINE_TMA;
+	fprintf(stderr, "Unknown B200_ENGINE=%s\n", s);
+	exit(1);
+}
+
 static int parse_init(const char* s)
 {
 	if (!s || !*s || !strcmp(s, "reference")) return KGH_INIT_REFERENCE;
@@ -107,6 +118,7 @@ int main(int argc, char* argv[])
 	const kg_dtype dt = parse_prec(getenv("B200_PREC"));
 	const int variant = parse_init(getenv("B200_INIT"));
 	const char* mode = getenv("B200_MODE");
+	const int engine = parse_engine(getenv("B200_ENGINE"));
 	const int graph = mode && !strcmp(mode, "graph");
 	if (dt == KG_U8 && test != KG_GAMEOFLIFE) { fprintf(stderr, "B200_PREC=u8 is for gameoflife only\n"); exit(1); }
 
@@ -178,6 +190,7 @@ int main(int argc, char* argv[])
 	memset(&p, 0, sizeof(p));
 	p.stencil = test;
 	p.dtype = dt;
+	p.engine = engine;
 	p.nx = nx;
 	p.ny = is2d ? ny : ny;
 	p.ns = ns;

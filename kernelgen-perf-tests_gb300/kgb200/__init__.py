@@ -37,8 +37,10 @@ EXPORTS = [
     "kg_device_check", "kg_version", "kg_measure_peaks", "kg_checksum_noalloc",
     "kg_batch_create", "kg_batch_step", "kg_batch_capture", "kg_batch_launch", "kg_batch_tune",
     "kg_batch_set_config", "kg_batch_get_config", "kg_batch_set_step", "kg_batch_final_roles",
-    "kg_batch_destroy", "kg_poisson_solve",
+    "kg_batch_destroy", "kg_poisson_solve", "kg_engine_status",
 ]
+KG_ENGINE_AUTO, KG_ENGINE_DIRECT, KG_ENGINE_STAGED, KG_ENGINE_TMA = 0, 1, 2, 3
+ENGINES = {"auto": KG_ENGINE_AUTO, "direct": KG_ENGINE_DIRECT, "staged": KG_ENGINE_STAGED, "tma": KG_ENGINE_TMA}
 KG_SOLVE_SOR_F64, KG_SOLVE_IR_SOR_F32, KG_SOLVE_IR_JACOBI_F32 = 0, 1, 2
 
 
@@ -52,7 +54,7 @@ class KgError(RuntimeError):
 class KgProblem(ctypes.Structure):
     _fields_ = [("stencil", ctypes.c_int32), ("dtype", ctypes.c_int32),
                 ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("ns", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("coef", ctypes.c_double * 6),
+                ("engine", ctypes.c_int32), ("coef", ctypes.c_double * 6),
                 ("arr", ctypes.c_void_p * 6)]
 
 
@@ -113,6 +115,7 @@ def _sig(lib):
         "kg_gaussblur": [I, I, I, D, D, D, D, D, D, P, P, P],
         "kg_gameoflife": [I, I, I, P, P, P],
         "kg_sweep": [ctypes.POINTER(KgProblem), P],
+        "kg_engine_status": [P],
         "kg_checksum": [I, S, I, ctypes.POINTER(ctypes.c_void_p), P, P],
         "kg_checksum_noalloc": [I, S, I, ctypes.POINTER(ctypes.c_void_p), P, P],
         "kg_error_stats": [I, S, P, P, P, P],
@@ -179,9 +182,11 @@ def stream_ptr(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
-def problem(stencil, dtype, shape, coef, arrays):
-    """kg_problem from a stencil name, dtype id, shape, coefficients and device pointers."""
+def problem(stencil, dtype, shape, coef, arrays, engine=KG_ENGINE_AUTO):
+    """kg_problem from a stencil name, dtype id, shape, coefficients and device
+    pointers; `engine` a KG_ENGINE_* id (or its name)."""
     p = KgProblem()
+    p.engine = ENGINES[engine] if isinstance(engine, str) else int(engine)
     p.stencil = STENCIL_ID[stencil] if isinstance(stencil, str) else int(stencil)
     p.dtype = dtype
     if len(shape) == 2:
@@ -197,6 +202,11 @@ def problem(stencil, dtype, shape, coef, arrays):
 
 def sweep(p, stream=None):
     check(load().kg_sweep(ctypes.byref(p), stream_ptr(stream)))
+
+
+def engine_status(stream=None):
+    """kg_engine_status: raises KgError(KG_ETIMEOUT) if a TMA sweep's wait gave up."""
+    check(load().kg_engine_status(stream_ptr(stream)))
 
 
 def checksum(dtype, n, arrays, out_ptr, stream=None):

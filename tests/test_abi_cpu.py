@@ -73,6 +73,18 @@ def test_bad_arguments_rejected_before_launch(lib):
     # bad plan arguments
     h = ctypes.c_void_p()
     assert lib.kg_plan_create(ctypes.byref(h), None, 3) == 1
+    # engines: unknown id, not built for the type, TMA on rows that are not
+    # a multiple of 16 bytes or on unaligned arrays
+    p = kgb200.problem("laplacian", kgb200.KG_F64, (8, 8, 8), [1.0, 1.0], [pa, pb], engine=7)
+    assert lib.kg_sweep(ctypes.byref(p), None) == 1 and b"unknown engine" in lib.kg_last_error()
+    p = kgb200.problem("laplacian", kgb200.KG_F64, (8, 8, 8), [1.0, 1.0], [pa, pb], engine="staged")
+    assert lib.kg_sweep(ctypes.byref(p), None) == 5
+    p = kgb200.problem("laplacian", kgb200.KG_U8, (8, 8, 8), [1.0, 1.0], [pa, pb], engine="tma")
+    assert lib.kg_sweep(ctypes.byref(p), None) == 5
+    p = kgb200.problem("laplacian", kgb200.KG_F32, (6, 8, 8), [1.0, 1.0], [pa, pb], engine="tma")
+    assert lib.kg_sweep(ctypes.byref(p), None) == 1 and b"16-byte" in lib.kg_last_error()
+    p = kgb200.problem("laplacian", kgb200.KG_F32, (8, 8, 8), [1.0, 1.0], [pa + 4, pb], engine="tma")
+    assert lib.kg_sweep(ctypes.byref(p), None) == 1 and b"16-byte" in lib.kg_last_error()
 
 
 def test_device_check_without_gpu(lib):
