@@ -134,13 +134,16 @@ template <class N> __device__ __forceinline__ void tricubic_weights(N a, N* w) {
 }
 
 // Strict FP64 tricubic: of the four x-neighbours ii of every (jj, kk) row,
-// the first kTricubicEmu have their *wc and *u0 products formed by the
-// exact integer multiply (se_mul).  Measured on GB300 (512x256x256, ms per
-// sweep): all on the FP64 unit 15.85; 1 of 4 13.65; 2 of 4 12.22; 3 of 4
-// 11.9; 4 of 4 25.6.  Moving part of the in-order sum, the weight
+// the first kTricubicEmuW have their *wc product and the first
+// kTricubicEmuU their *u0 product formed by the exact integer multiply
+// (se_mul).  Measured on GB300 (512x256x256, ms per sweep): all on the FP64
+// unit 15.85; 1 of 4 13.65; 2 of 4 12.22; 3 of 4 11.9; 4 of 4 25.6; 4 and 3
+// 12.5; 3 and 4 12.3.  The kernel holds 116 registers (two CTAs of 256
+// threads per SM); capping it at 85 (three CTAs) gave 14.0, letting it take
+// 156 (one CTA) 21.1.  Moving part of the in-order sum, the weight
 // polynomials or the wa*wb products as well was slower (those are
 // dependent chains, and the integer operations' latency then shows).
-constexpr int kTricubicEmu = 3;
+constexpr int kTricubicEmuW = 3, kTricubicEmuU = 3;
 
 // tricubic/tricubic.c:1062-1145 (64 terms, t0 + t1 + ... + t63, x fastest)
 // and tricubic2/tricubic2.c:98-102 (u1 = 0; u1 += t_n, same term order).
@@ -177,8 +180,8 @@ template <class N, bool FROM_ZERO> struct OpTricubicT {
 					for (int ii = 0; ii < 4; ii++) {
 						const double u = at(u0, ii - 1, jj - 1, kk - 1).v;
 						const double w = wab[jj * 4 + ii];
-						const double pw = ii < kTricubicEmu ? se_mul(w, wc[kk].v) : __dmul_rn(w, wc[kk].v);
-						const double t = ii < kTricubicEmu ? se_mul(pw, u) : __dmul_rn(pw, u);
+						const double pw = ii < kTricubicEmuW ? se_mul(w, wc[kk].v) : __dmul_rn(w, wc[kk].v);
+						const double t = ii < kTricubicEmuU ? se_mul(pw, u) : __dmul_rn(pw, u);
 						if (kk == 0 && jj == 0 && ii == 0)
 							s = FROM_ZERO ? __dadd_rn(0.0, t) : t;
 						else
