@@ -119,6 +119,42 @@ kg_status kg_gaussblur(kg_dtype dt, int nx, int ny,
 kg_status kg_gameoflife(kg_dtype dt, int nx, int ny,
 	const void* u0, void* u1, kg_stream_t stream);
 
+/* ---- the suite's other tests (not stencil sweeps) ---------------------- */
+/* KG_F64 (strict IEEE, bit for bit the reference expression in its loop
+ * order), KG_F64_FMA or KG_F32; device pointers; asynchronous on `stream`. */
+
+/* vecadd/vecadd.c:38-84: w2 = w0 + w1 at every point. */
+kg_status kg_vecadd(kg_dtype dt, int nx, int ny, int ns,
+	const void* w0, const void* w1, void* w2, kg_stream_t stream);
+
+/* matvec/matvec.c:37-71: y[j] = sum over i of A[i + nx*j] * x[i], summed
+ * in order i = 0, 1, ... from y[j] = 0. */
+kg_status kg_matvec(kg_dtype dt, int nx, int ny,
+	const void* A, const void* x, void* y, kg_stream_t stream);
+
+/* matmul/matmul.F90:14-68 (column-major, as the Fortran kernel): C(i,j) =
+ * C(i,j) + A(i,k) * B(k,j) in order k = 1..ny, with A(i,k) at A[i + nx*k],
+ * B(k,j) at B[k + ny*j], C(i,j) at C[i + nx*j]; C accumulates (the caller
+ * sets its initial value). */
+kg_status kg_matmul(kg_dtype dt, int nx, int ny, int ns,
+	const void* A, const void* B, void* C, kg_stream_t stream);
+
+/* sincos/sincos.F90:60-72: xy = sin(x) + cos(y) at every point (CUDA's
+ * sin/cos: within 2 ulp of the correctly rounded values, not bitwise). */
+kg_status kg_sincos(kg_dtype dt, int nx, int ny, int ns,
+	const void* x, const void* y, void* xy, kg_stream_t stream);
+
+/* whispering/whispering.c:44-108: one step on [1,nx-2] x [1,ny-2]; e holds
+ * two planes (component c of (i,j) at e[i + nx*j + nx*ny*c]) and is updated
+ * in place with the result of the reference's serial loop order (its ey and
+ * ex terms read e already updated at (i,j-1) and (i-1,j)). */
+kg_status kg_whispering(kg_dtype dt, int nx, int ny, double mu, double epsilon,
+	void* e, const void* h0, void* h1, const void* u_em0, void* u_em1,
+	const void* ca, const void* cb, const void* da, const void* db, kg_stream_t stream);
+
+/* Registers per thread of the main kernel of the named test above. */
+kg_status kg_extra_regcount(const char* name, kg_dtype dt, int* nregs);
+
 /* ---- table-driven form of the same entry points ------------------------ */
 
 /* Which kernel design runs a sweep (kg_problem.engine).  AUTO: TMA for

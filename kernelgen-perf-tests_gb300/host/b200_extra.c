@@ -1,0 +1,293 @@
+/*
+ * b200_extra.c -- the b200 target program of one of the suite's tests that
+ * are not stencil sweeps (KG_TEST_NAME: vecadd, matvec, matmul, sincos,
+ * whispering).
+ *
+ * Same command line, rand() draws, phases and stdout lines as the reference
+ * main() of the test (vecadd/vecadd.c:97-380, matvec/matvec.c:82-350,
+ * matmul/main.c:54-320, sincos/main.c:59-320, whispering/whispering.c:
+ * 120-480), so the suite's `benchmark` harness parses it; the steps run on
+ * the GPU through the kg_b200 C ABI.  The printed means are summed on the
+ * host in the reference's order from the arrays copied back.
+ *
+ * Knobs: B200_PREC fp64 (default; strict IEEE) | fp64fma | fp32;
+ *        NO_TIMING, PROFILING_FNAME as in the reference.
+ * matmul: the reference leaves C unset before accumulating into it; here C
+ * starts at zero, the content of freshly mapped memory.
+ */
+#include <malloc.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "kg_b200.h"
+#include "kg_host.h"
+
+#define MEMALIGN 4096
+
+#define KG_CHECK(x) do { kg_status s_ = (x); if (s_ != KG_OK) { \
+	fprintf(stderr, "Error \"%s: %s\" in %s\n", kg_status_string(s_), kg_last_error(), #x); exit(-1); } } while (0)
+#define CU_CHECK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { \
+	fprintf(stderr, "Error \"%s\" in %s\n", cudaGetErrorString(e_), #x); exit(-1); } } while (0)
+
+enum { T_VECADD, T_MATVEC, T_MATMUL, T_SINCOS, T_WHISPERING };
+
+static int test_id(const char* s)
+{
+	static const char* names[] = {"vecadd", "matvec", "matmul", "sincos", "whispering"};
+	for (int t = 0; t < 5; t++)
+		if (!strcmp(s, names[t])) return t;
+	return -1;
+}
+
+static int parse_arg(const char* name, const char* arg)
+{
+	const int v = atoi(arg);
+	if (v < 0) {
+		printf("Value for %s is invalid: %d\n", name, v);
+		exit(1);
+	}
+	return v;
+}
+
+static kg_dtype parse_prec(const char* s)
+{
+	if (!s || !*s || !strcmp(s, "fp64")) return KG_F64;
+	if (!strcmp(s, "fp64fma")) return KG_F64_FMA;
+	if (!strcmp(s, "fp32")) return KG_F32;
+	fprintf(stderr, "Unknown B200_PREC=%s (fp64 | fp64fma | fp32)\n", s);
+	exit(1);
+}
+
+static kgh_rng g_rng;
+/* laplacian/laplacian.c:112 real_rand() with real = double (every test's own copy). */
+static double real_rand(void)
+{
+	return ((double)(kgh_rng_next(&g_rng) / (double)2147483647) - 0.5) * 2;
+}
+
+/* One host array of n doubles and its device twin. */
+typedef struct {
+	size_t n;
+	double* h;
+	void* d;
+} arr_t;
+
+int main(int argc, char* argv[])
+{
+	const int test = test_id(KG_TEST_NAME);
+	if (test < 0) { fprintf(stderr, "unknown test %s\n", KG_TEST_NAME); return 1; }
+	const int three = test == T_MATVEC || test == T_WHISPERING;   /* nx ny nt */
+	if (argc != (three ? 4 : 5)) {
+		if (three) printf("Usage: %s <nx> <ny> <nt>\n", argv[0]);
+		else printf("Usage: %s <nx> <ny> <ns> <nt>\n", argv[0]);
+		exit(1);
+	}
+	const char* no_timing = getenv("NO_TIMING");
+	const char* prof_name = getenv("PROFILING_FNAME");
+	const kg_dtype dt = parse_prec(getenv("B200_PREC"));
+	const size_t es = dt == KG_F32 ? 4 : 8;
+
+	const int nx = parse_arg("nx", argv[1]);
+	const int ny = parse_arg("ny", argv[2]);
+	const int ns = three ? 1 : parse_arg("ns", argv[3]);
+	const int nt = parse_arg("nt", argv[three ? 3 : 4]);
+	const size_t n = (size_t)nx * ny * ns;
+
+	/* arrays in the reference's allocation order */
+	arr_t a[9];
+	int na = 0;
+	memset(a, 0, sizeof(a));
+	switch (test) {
+	case T_VECADD: case T_SINCOS: na = 3; for (int q = 0; q < 3; q++) a[q].n = n; break;
+	case T_MATVEC: na = 3; a[0].n = (size_t)nx * ny; a[1].n = nx; a[2].n = ny; break;
+	case T_MATMUL: na = 3; a[0].n = (size_t)nx * ny; a[1].n = (size_t)ny * ns; a[2].n = (size_t)nx * ns; break;
+	case T_WHISPERING: na = 9; a[0].n = 2 * n; for (int q = 1; q < 9; q++) a[q].n = n; break;
+	}
+	for (int q = 0; q < na; q++) {
+		a[q].h = (double*)memalign(MEMALIGN, a[q].n ? a[q].n * sizeof(double) : 8);
+		if (!a[q].h) { printf("Error allocating memory for arrays\n"); exit(1); }
+	}
+
+	/* draws and initial mean */
+	kgh_rng_seed(&g_rng, 1u);
+	double mu = 0, epsilon = 0, imean = 0;
+	switch (test) {
+	case T_VECADD: case T_SINCOS: {          /* vecadd/vecadd.c:137-145, sincos/main.c:99-107 */
+		double m = 0.0;
+		for (size_t i = 0; i < n; i++) {
+			a[0].h[i] = real_rand(); a[1].h[i] = real_rand(); a[2].h[i] = real_rand();
+			m += a[0].h[i] + a[1].h[i] + a[2].h[i];
+		}
+		imean = m / n / 3;
+		break;
+	}
+	case T_MATVEC: {                         /* matvec/matvec.c:120-139 */
+		double am = 0.0, xm = 0.0, ym = 0.0;
+		for (size_t i = 0; i < a[0].n; i++) { a[0].h[i] = real_rand(); am += a[0].h[i]; }
+		for (size_t i = 0; i < a[1].n; i++) { a[1].h[i] = real_rand(); xm += a[1].h[i]; }
+		for (size_t i = 0; i < a[2].n; i++) { a[2].h[i] = real_rand(); ym += a[2].h[i]; }
+		imean = am / (nx * ny) + xm / nx + ym / ny;
+		break;
+	}
+	case T_MATMUL: {                         /* matmul/main.c:98-110 */
+		double ma = 0.0, mb = 0.0;
+		for (size_t i = 0; i < a[0].n; i++) { a[0].h[i] = real_rand(); ma += a[0].h[i]; }
+		for (size_t i = 0; i < a[1].n; i++) { a[1].h[i] = real_rand(); mb += a[1].h[i]; }
+		memset(a[2].h, 0, a[2].n * sizeof(double));
+		imean = ma / a[0].n + mb / a[1].n;
+		break;
+	}
+	case T_WHISPERING: {                     /* whispering/whispering.c:148-190 */
+		mu = real_rand();
+		epsilon = real_rand();
+		printf("mu = %f, epsilon = %f\n", mu, epsilon);
+		double m = 0.0;
+		for (size_t i = 0; i < n; i++) {
+			a[0].h[2 * i] = real_rand();
+			a[0].h[2 * i + 1] = real_rand();
+			for (int q = 1; q < 9; q++) a[q].h[i] = real_rand();
+			m += a[0].h[2 * i] + a[0].h[2 * i + 1] + a[1].h[i] + a[2].h[i] + a[3].h[i] + a[4].h[i] +
+				a[5].h[i] + a[6].h[i] + a[7].h[i] + a[8].h[i];
+		}
+		imean = m / n / 12;
+		break;
+	}
+	}
+	/* vecadd and matvec print it only with timing on (vecadd/vecadd.c:145,
+	 * matvec/matvec.c:140); the others always. */
+	if (!no_timing || !(test == T_VECADD || test == T_MATVEC)) printf("initial mean = %f\n", imean);
+
+	struct timespec t0, t1;
+	kgh_get_time(&t0);
+	int count = 0;
+	CU_CHECK(cudaGetDeviceCount(&count));
+	KG_CHECK(kg_device_check());
+	kgh_get_time(&t1);
+	if (!no_timing) printf("init time = %f sec\n", kgh_time_diff(&t0, &t1));
+
+	kgh_get_time(&t0);
+	for (int q = 0; q < na; q++) CU_CHECK(cudaMalloc(&a[q].d, a[q].n ? a[q].n * es : 8));
+	float* stage = NULL;   /* FP32 form: conversion on the host */
+	size_t maxn = 0;
+	for (int q = 0; q < na; q++) maxn = a[q].n > maxn ? a[q].n : maxn;
+	if (es == 4) stage = (float*)malloc((maxn ? maxn : 1) * sizeof(float));
+	kgh_get_time(&t1);
+	if (!no_timing) printf("device buffer alloc time = %f sec\n", kgh_time_diff(&t0, &t1));
+
+	kgh_get_time(&t0);
+	size_t loaded = 0;
+	for (int q = 0; q < na; q++) {
+		if (es == 8) {
+			CU_CHECK(cudaMemcpy(a[q].d, a[q].h, a[q].n * 8, cudaMemcpyHostToDevice));
+		} else {
+			for (size_t i = 0; i < a[q].n; i++) stage[i] = (float)a[q].h[i];
+			CU_CHECK(cudaMemcpy(a[q].d, stage, a[q].n * 4, cudaMemcpyHostToDevice));
+		}
+		loaded += a[q].n * es;
+	}
+	kgh_get_time(&t1);
+	double load_t = kgh_time_diff(&t0, &t1);
+	if (!no_timing) printf("data load time = %f sec (%f GB/sec)\n", load_t, loaded / (load_t * 1024 * 1024 * 1024));
+
+	if (prof_name) {
+		int nregs = 0;
+		KG_CHECK(kg_extra_regcount(KG_TEST_NAME, dt, &nregs));
+		printf("%s regcount = %d\n", prof_name, nregs);
+	}
+	void* p[9];
+	for (int q = 0; q < na; q++) p[q] = a[q].d;
+	cudaEvent_t* ev = (cudaEvent_t*)malloc(sizeof(cudaEvent_t) * (2 * (size_t)nt + 2));
+	for (int it = 0; it < 2 * nt; it++) CU_CHECK(cudaEventCreate(&ev[it]));
+	kgh_get_time(&t0);
+	for (int it = 0; it < nt; it++) {
+		CU_CHECK(cudaEventRecord(ev[2 * it], 0));
+		switch (test) {
+		case T_VECADD: KG_CHECK(kg_vecadd(dt, nx, ny, ns, p[0], p[1], p[2], 0)); break;
+		case T_SINCOS: KG_CHECK(kg_sincos(dt, nx, ny, ns, p[0], p[1], p[2], 0)); break;
+		case T_MATVEC: KG_CHECK(kg_matvec(dt, nx, ny, p[0], p[1], p[2], 0)); break;
+		case T_MATMUL: KG_CHECK(kg_matmul(dt, nx, ny, ns, p[0], p[1], p[2], 0)); break;
+		case T_WHISPERING:
+			KG_CHECK(kg_whispering(dt, nx, ny, mu, epsilon, p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], 0));
+			break;
+		}
+		CU_CHECK(cudaEventRecord(ev[2 * it + 1], 0));
+		/* the reference's rotation (vecadd/vecadd.c:278; whispering.c:368-369) */
+		if (test == T_VECADD) { void* t = p[0]; p[0] = p[1]; p[1] = p[2]; p[2] = t; }
+		if (test == T_WHISPERING) {
+			void* t = p[1]; p[1] = p[2]; p[2] = t;
+			t = p[3]; p[3] = p[4]; p[4] = t;
+		}
+	}
+	CU_CHECK(cudaDeviceSynchronize());
+	kgh_get_time(&t1);
+	const double compute_t = kgh_time_diff(&t0, &t1);
+	if (prof_name)
+		for (int it = 0; it < nt; it++) {
+			float ms = 0;
+			CU_CHECK(cudaEventElapsedTime(&ms, ev[2 * it], ev[2 * it + 1]));
+			printf("%s kernel time = %f\n", prof_name, ms * 1e-3);
+		}
+	if (!no_timing) printf("compute time = %f sec\n", compute_t);
+	for (int it = 0; it < 2 * nt; it++) cudaEventDestroy(ev[it]);
+	free(ev);
+
+	/* save: the arrays the final mean reads, in their final roles */
+	int fin[3], nfin = 0;
+	switch (test) {
+	case T_VECADD: fin[nfin++] = 1; break;
+	case T_MATVEC: case T_MATMUL: case T_SINCOS: fin[nfin++] = 2; break;
+	case T_WHISPERING: fin[nfin++] = 0; fin[nfin++] = 2; fin[nfin++] = 4; break;
+	}
+	double* out[3];
+	kgh_get_time(&t0);
+	size_t saved = 0;
+	for (int f = 0; f < nfin; f++) {
+		const int q = fin[f];
+		/* the array now in role q: its host twin is the one allocated with that device buffer */
+		int src = 0;
+		for (int r = 0; r < na; r++) if (a[r].d == p[q]) src = r;
+		out[f] = a[src].h;
+		if (es == 8) {
+			CU_CHECK(cudaMemcpy(out[f], p[q], a[src].n * 8, cudaMemcpyDeviceToHost));
+		} else {
+			CU_CHECK(cudaMemcpy(stage, p[q], a[src].n * 4, cudaMemcpyDeviceToHost));
+			for (size_t i = 0; i < a[src].n; i++) out[f][i] = stage[i];
+		}
+		saved += a[src].n * es;
+	}
+	kgh_get_time(&t1);
+	double save_t = kgh_time_diff(&t0, &t1);
+	if (!no_timing) printf("data save time = %f sec (%f GB/sec)\n", save_t, saved / (save_t * 1024 * 1024 * 1024));
+
+	kgh_get_time(&t0);
+	for (int q = 0; q < na; q++) CU_CHECK(cudaFree(a[q].d));
+	kgh_get_time(&t1);
+	if (!no_timing) printf("device buffer free time = %f sec\n", kgh_time_diff(&t0, &t1));
+
+	double mean = 0.0;
+	switch (test) {
+	case T_VECADD: case T_SINCOS:
+		for (size_t i = 0; i < n; i++) mean += out[0][i];
+		printf("final mean = %f\n", mean / n);
+		break;
+	case T_MATVEC:
+		for (int i = 0; i < ny; i++) mean += out[0][i];
+		printf("final mean = %f\n", mean / ny);
+		break;
+	case T_MATMUL:
+		for (size_t i = 0; i < (size_t)nx * ns; i++) mean += out[0][i];
+		printf("final mean = %f\n", mean / ((size_t)nx * ns));
+		break;
+	case T_WHISPERING:
+		for (size_t i = 0; i < n; i++) mean += out[0][2 * i] + out[0][2 * i + 1] + out[1][i] + out[2][i];
+		printf("final mean = %f\n", mean / n / 4);
+		break;
+	}
+	for (int q = 0; q < na; q++) free(a[q].h);
+	free(stage);
+	fflush(stdout);
+	return 0;
+}

@@ -38,7 +38,9 @@ EXPORTS = [
     "kg_batch_create", "kg_batch_step", "kg_batch_capture", "kg_batch_launch", "kg_batch_tune",
     "kg_batch_set_config", "kg_batch_get_config", "kg_batch_set_step", "kg_batch_final_roles",
     "kg_batch_destroy", "kg_poisson_solve", "kg_engine_status",
+    "kg_vecadd", "kg_matvec", "kg_matmul", "kg_sincos", "kg_whispering", "kg_extra_regcount",
 ]
+EXTRA_TESTS = ["vecadd", "matvec", "matmul", "sincos", "whispering"]
 KG_ENGINE_AUTO, KG_ENGINE_DIRECT, KG_ENGINE_STAGED, KG_ENGINE_TMA = 0, 1, 2, 3
 ENGINES = {"auto": KG_ENGINE_AUTO, "direct": KG_ENGINE_DIRECT, "staged": KG_ENGINE_STAGED, "tma": KG_ENGINE_TMA}
 KG_SOLVE_SOR_F64, KG_SOLVE_IR_SOR_F32, KG_SOLVE_IR_JACOBI_F32 = 0, 1, 2
@@ -116,6 +118,12 @@ def _sig(lib):
         "kg_gameoflife": [I, I, I, P, P, P],
         "kg_sweep": [ctypes.POINTER(KgProblem), P],
         "kg_engine_status": [P],
+        "kg_vecadd": [I, I, I, I, P, P, P, P],
+        "kg_matvec": [I, I, I, P, P, P, P],
+        "kg_matmul": [I, I, I, I, P, P, P, P],
+        "kg_sincos": [I, I, I, I, P, P, P, P],
+        "kg_whispering": [I, I, I, D, D] + [P] * 9 + [P],
+        "kg_extra_regcount": [ctypes.c_char_p, I, ctypes.POINTER(I)],
         "kg_checksum": [I, S, I, ctypes.POINTER(ctypes.c_void_p), P, P],
         "kg_checksum_noalloc": [I, S, I, ctypes.POINTER(ctypes.c_void_p), P, P],
         "kg_error_stats": [I, S, P, P, P, P],
@@ -202,6 +210,36 @@ def problem(stencil, dtype, shape, coef, arrays, engine=KG_ENGINE_AUTO):
 
 def sweep(p, stream=None):
     check(load().kg_sweep(ctypes.byref(p), stream_ptr(stream)))
+
+
+def extra_step(test, dtype, args, ptrs, coef=(), stream=None):
+    """One call of kg_<test> (vecadd, matvec, matmul, sincos, whispering) on
+    device pointers; args are the sizes of its command line (without nt)."""
+    lib = load()
+    st = stream_ptr(stream)
+    if test == "vecadd":
+        check(lib.kg_vecadd(dtype, *args, *ptrs, st))
+    elif test == "sincos":
+        check(lib.kg_sincos(dtype, *args, *ptrs, st))
+    elif test == "matvec":
+        check(lib.kg_matvec(dtype, *args, *ptrs, st))
+    elif test == "matmul":
+        check(lib.kg_matmul(dtype, *args, *ptrs, st))
+    elif test == "whispering":
+        check(lib.kg_whispering(dtype, args[0], args[1], coef[0], coef[1], *ptrs, st))
+    else:
+        raise ValueError(test)
+
+
+def extra_rotate(test, ptrs):
+    """The reference main()'s pointer rotation after one step."""
+    p = list(ptrs)
+    if test == "vecadd":
+        return [p[1], p[2], p[0]]
+    if test == "whispering":   # e, h0, h1, u_em0, u_em1, ...
+        p[1], p[2] = p[2], p[1]
+        p[3], p[4] = p[4], p[3]
+    return p
 
 
 def engine_status(stream=None):

@@ -6,7 +6,8 @@
 #   cd <output-dir> && ./benchmark 512 256 256 10 10 gcc b200
 #
 # Copies the reference tree, drops a b200/ directory (makefile + kernel file)
-# into each stencil test, writes makefile.b200.in with this package's path, and
+# into each test the target covers (the eleven stencil tests, vecadd, matvec,
+# matmul, sincos, whispering), writes makefile.b200.in with this package's path, and
 # applies benchmark.patch (the harness parses b200's kernel-time and regcount
 # lines, as it does for cuda) and makefile.patch (%.b200 and test.b200 rules).
 set -e
@@ -24,7 +25,8 @@ if [ -e "$OUT" ]; then
 fi
 cp -R "$REF" "$OUT"
 chmod -R u+w "$OUT"
-for t in laplacian divergence gradient uxx1 wave13pt tricubic tricubic2 jacobi lapgsrb gaussblur gameoflife; do
+for t in laplacian divergence gradient uxx1 wave13pt tricubic tricubic2 jacobi lapgsrb gaussblur gameoflife \
+	vecadd matvec matmul sincos whispering; do
 	cp -R "$HERE/$t/b200" "$OUT/$t/b200"
 done
 sed "s|@KG_ROOT@|$KG|" "$HERE/makefile.b200.in" > "$OUT/makefile.b200.in"

@@ -115,6 +115,21 @@ double or_residual_norm(int nx, int ny, int ns, const double* u, const double* f
 /* Plain FP64 serial sum of x[0..n). */
 double or_sum(const double* x, size_t n);
 
+/* ---- the suite's other tests (kg_oracle_extra.c) ------------------------ */
+void or_vecadd(size_t n, const double* w0, const double* w1, double* w2);
+void or_matvec(int nx, int ny, const double* A, const double* x, double* y);
+void or_matmul(int nx, int ny, int ns, const double* A, const double* B, double* C);
+void or_sincos(size_t n, const double* x, const double* y, double* xy);
+void or_whispering(int nx, int ny, double mu, double epsilon, double* e, const double* h0, double* h1,
+	const double* u_em0, double* u_em1, const double* ca, const double* cb, const double* da, const double* db);
+/* Whole programs (reference draws, time loop, means); w / a permuted into
+ * their final roles. */
+void or_vecadd_program(int nx, int ny, int ns, int nt, double** w, double* imean, double* fmean);
+void or_matvec_program(int nx, int ny, int nt, double* A, double* x, double* y, double* imean, double* fmean);
+void or_matmul_program(int nx, int ny, int ns, int nt, double* A, double* B, double* C, double* imean, double* fmean);
+void or_sincos_program(int nx, int ny, int ns, int nt, double* x, double* y, double* xy, double* imean, double* fmean);
+void or_whispering_program(int nx, int ny, int nt, double* coef, double** a, double* imean, double* fmean);
+
 #ifdef __cplusplus
 }
 #endif

@@ -153,3 +153,73 @@ def bernoulli_u8(n, p=0.3, seed=1):
     u1 = np.zeros(n, dtype=np.uint8)
     lib.or_init_bernoulli_u8(n, u0.ctypes.data, u1.ctypes.data, p, seed)
     return u0, u1
+
+
+# ---- the suite's other tests (oracle/kg_oracle_extra.c) ----------------------
+
+EXTRA = ["vecadd", "matvec", "matmul", "sincos", "whispering"]
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def extra_program(test, args, flavour="strict"):
+    """Run one of the other tests as the reference main() does.  args as its
+    command line (vecadd/sincos/matmul: nx ny ns nt; matvec/whispering: nx
+    ny nt).  Returns (arrays in their final roles, coefficients, initial mean,
+    final mean); the arrays are those the test allocates, in its order."""
+    lib = load(flavour)
+    im, fm = ctypes.c_double(), ctypes.c_double()
+    coef = []
+    if test in ("vecadd", "sincos"):
+        nx, ny, ns, nt = args
+        n = nx * ny * ns
+        a = [np.empty(n) for _ in range(3)]
+        if test == "vecadd":
+            w = (ctypes.POINTER(ctypes.c_double) * 3)(*[_dp(x) for x in a])
+            lib.or_vecadd_program(nx, ny, ns, nt, w, ctypes.byref(im), ctypes.byref(fm))
+            order = [next(q for q in range(3) if ctypes.addressof(w[r].contents) == a[q].ctypes.data)
+                     for r in range(3)]
+            a = [a[q] for q in order]
+        else:
+            lib.or_sincos_program(nx, ny, ns, nt, _dp(a[0]), _dp(a[1]), _dp(a[2]), ctypes.byref(im), ctypes.byref(fm))
+    elif test == "matvec":
+        nx, ny, nt = args
+        a = [np.empty(nx * ny), np.empty(nx), np.empty(ny)]
+        lib.or_matvec_program(nx, ny, nt, _dp(a[0]), _dp(a[1]), _dp(a[2]), ctypes.byref(im), ctypes.byref(fm))
+    elif test == "matmul":
+        nx, ny, ns, nt = args
+        a = [np.empty(nx * ny), np.empty(ny * ns), np.empty(nx * ns)]
+        lib.or_matmul_program(nx, ny, ns, nt, _dp(a[0]), _dp(a[1]), _dp(a[2]), ctypes.byref(im), ctypes.byref(fm))
+    elif test == "whispering":
+        nx, ny, nt = args
+        n = nx * ny
+        a = [np.empty(2 * n)] + [np.empty(n) for _ in range(8)]
+        c = (ctypes.c_double * 2)()
+        w = (ctypes.POINTER(ctypes.c_double) * 9)(*[_dp(x) for x in a])
+        lib.or_whispering_program(nx, ny, nt, c, w, ctypes.byref(im), ctypes.byref(fm))
+        by_addr = {x.ctypes.data: x for x in a}
+        a = [by_addr[ctypes.addressof(w[r].contents)] for r in range(9)]
+        coef = list(c)
+    else:
+        raise ValueError(test)
+    return a, coef, im.value, fm.value
+
+
+def extra_step(test, arrays, args, coef=()):
+    """One step of the oracle kernel on numpy arrays (in place)."""
+    lib = load("strict")
+    if test == "vecadd":
+        lib.or_vecadd(ctypes.c_size_t(arrays[0].size), *[_dp(x) for x in arrays])
+    elif test == "sincos":
+        lib.or_sincos(ctypes.c_size_t(arrays[0].size), *[_dp(x) for x in arrays])
+    elif test == "matvec":
+        lib.or_matvec(args[0], args[1], *[_dp(x) for x in arrays])
+    elif test == "matmul":
+        lib.or_matmul(args[0], args[1], args[2], *[_dp(x) for x in arrays])
+    elif test == "whispering":
+        lib.or_whispering(args[0], args[1], ctypes.c_double(coef[0]), ctypes.c_double(coef[1]),
+                          *[_dp(x) for x in arrays])
+    else:
+        raise ValueError(test)
