@@ -680,6 +680,67 @@ def run_e2e(args, dtype, lanes=E2E_LANES):
     return dt, h2d, d2h
 
 
+# ---- the suite's other tests (vecadd, matvec, matmul, sincos, whispering) ----
+
+OTHER = {   # command line of the suite's own size; compulsory bytes and FP64 operations per step
+    "vecadd": ((512, 256, 256), lambda a: 24 * a[0] * a[1] * a[2], lambda a: a[0] * a[1] * a[2]),
+    "matvec": ((512, 65536), lambda a: 8 * (a[0] * a[1] + a[0] + a[1]), lambda a: 2 * a[0] * a[1]),
+    "matmul": ((512, 256, 256), lambda a: 8 * (a[0] * a[1] + a[1] * a[2] + 2 * a[0] * a[2]),
+               lambda a: 2 * a[0] * a[1] * a[2]),
+    "sincos": ((512, 256, 256), lambda a: 24 * a[0] * a[1] * a[2], lambda a: 0),
+    "whispering": ((512, 65536), lambda a: 96 * a[0] * a[1], lambda a: 33 * a[0] * a[1]),
+}
+
+
+def run_other(reps=10):
+    """Device time of one step of each test at the suite's size (strict FP64 and
+    FP32), with the roofline of its bound, and the oracle's fast-math build on
+    the host cores for a CPU reference point."""
+    import numpy as np
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+
+    hbm_peak, _ = peaks()
+    out = {}
+    for name, (args, nbytes, nops) in OTHER.items():
+        init, coef, _, _ = ol.extra_program(name, tuple(args) + (0,), flavour="fast")
+        row = {"args": list(args)}
+        for dname, dt, tdt in (("f64", kgb200.KG_F64, torch.float64), ("f32", kgb200.KG_F32, torch.float32)):
+            bufs = [torch.from_numpy(a).cuda().to(tdt) for a in init]
+            ptrs = [b.data_ptr() for b in bufs]
+            for _ in range(2):
+                kgb200.extra_step(name, dt, args, ptrs, coef)
+            torch.cuda.synchronize()
+            best = 1e30
+            for _ in range(3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    kgb200.extra_step(name, dt, args, ptrs, coef)
+                e1.record()
+                torch.cuda.synchronize()
+                best = min(best, e0.elapsed_time(e1) / reps * 1e-3)
+            b = nbytes(args) * (4 if dt == kgb200.KG_F32 else 8) / 8
+            r = {"ms_per_step": round(best * 1e3, 4), "hbm_gbs": round(b / best / 1e9, 1),
+                 "hbm_frac_of_measured": round(b / best / 1e9 / hbm_peak, 3)}
+            if dt == kgb200.KG_F64 and nops(args):
+                r["fp64_tops"] = round(nops(args) / best / 1e12, 3)
+            row[dname] = r
+            del bufs
+        t0 = time.perf_counter()
+        ol.extra_program(name, tuple(args) + (1,), flavour="fast")
+        t1 = time.perf_counter()
+        ol.extra_program(name, tuple(args) + (0,), flavour="fast")
+        t2 = time.perf_counter()
+        row["cpu_oracle_ms_per_step"] = round(max((t1 - t0) - (t2 - t1), 1e-9) * 1e3, 2)
+        row["speedup_f64_vs_cpu"] = round(row["cpu_oracle_ms_per_step"] / row["f64"]["ms_per_step"], 1)
+        out[name] = row
+    out["note"] = ("one step at the suite's problem size; KG_F64 bitwise equal to the oracle; CPU: the oracle's "
+                   "fast-math build on the host cores (step time = program time minus its init)")
+    return out
+
+
 # ---- CPU baseline (the oracle built with the suite's flags) ---------------
 
 def cpu_cases():
@@ -896,6 +957,7 @@ def main():
         line["forms"]["iterative_refinement"] = dict(
             note="measured to tolerance on 192x192x128; the 768x768x512 run is bench.py --workload ir",
             **run_ir(IR_SMALL))
+        line["other_tests"] = run_other()
     if args.rank == 0 and args.world == 1 and not args.no_cpu:
         lib, cases, keep = cpu_cases()
         g, threads, sample = cpu_sweeps(lib, cases, repeats=3, seconds_cap=25.0)

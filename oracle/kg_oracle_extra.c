@@ -7,7 +7,9 @@
  * reproduces the reference main(): rand() draws in its order (the reference
  * never seeds: srand(1)), the time loop with its pointer rotation, and the
  * printed means with its accumulation order.  Citations are file:line inside
- * the reference project.
+ * the reference project.  Loops whose outputs are independent run as OpenMP
+ * loops (each output is computed exactly as in the serial loop); whispering's
+ * in-place loop stays serial.
  *
  * Pins: vecadd, matvec and whispering are C in the reference and are checked
  * against its own sources compiled unmodified (tests/golden/
@@ -32,12 +34,14 @@ static double real_rand(void)
 /* vecadd/vecadd.c:38-84 */
 void or_vecadd(size_t n, const double* w0, const double* w1, double* w2)
 {
+	#pragma omp parallel for
 	for (size_t i = 0; i < n; i++) w2[i] = w0[i] + w1[i];
 }
 
 /* matvec/matvec.c:37-71: y[j] = 0; y[j] += A[i + nx*j] * x[i] */
 void or_matvec(int nx, int ny, const double* A, const double* x, double* y)
 {
+	#pragma omp parallel for
 	for (int j = 0; j < ny; j++) {
 		double s = 0;
 		for (int i = 0; i < nx; i++) s += A[i + (size_t)nx * j] * x[i];
@@ -48,6 +52,7 @@ void or_matvec(int nx, int ny, const double* A, const double* x, double* y)
 /* matmul/matmul.F90:56-68, column-major: C(i,j) = C(i,j) + A(i,k) * B(k,j). */
 void or_matmul(int nx, int ny, int ns, const double* A, const double* B, double* C)
 {
+	#pragma omp parallel for
 	for (int j = 0; j < ns; j++)
 		for (int i = 0; i < nx; i++) {
 			double c = C[i + (size_t)nx * j];
@@ -59,6 +64,7 @@ void or_matmul(int nx, int ny, int ns, const double* A, const double* B, double*
 /* sincos/sincos.F90:60-72 */
 void or_sincos(size_t n, const double* x, const double* y, double* xy)
 {
+	#pragma omp parallel for
 	for (size_t i = 0; i < n; i++) xy[i] = sin(x[i]) + cos(y[i]);
 }
 
