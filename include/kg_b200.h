@@ -279,7 +279,8 @@ kg_status kg_plan_destroy(kg_plan plan);
  * No counterpart in the reference (each suite program runs one problem). */
 typedef struct kg_batch_s* kg_batch;
 typedef struct {
-	int shape, bx, by, kc;   /* tile shape: BX x BY threads, KC planes (rows in 2D) */
+	int shape, bx, by, kc;   /* tile: BX*BY threads on as many consecutive (i,j)
+	                            columns, KC planes each (2D: KC runs of points) */
 	int ctas_per_sm;
 	int tiles;               /* tiles of all problems per step */
 	int nshapes;             /* tile shapes the tuner tries */
@@ -293,8 +294,8 @@ kg_status kg_batch_step(kg_batch b, int nsteps, kg_stream_t stream);
  * kg_batch_launch replays it and continues from the current step. */
 kg_status kg_batch_capture(kg_batch b, int nsteps);
 kg_status kg_batch_launch(kg_batch b, kg_stream_t stream);
-/* Times every tile shape x {2,4,8} CTAs/SM on this batch (advancing it) and
- * keeps the fastest; cache_path (may be NULL) stores and reuses the choice
+/* Times every tile shape with as many CTAs per SM as stay resident, one
+ * fewer and half as many, on this batch (advancing it), and keeps the fastest; cache_path (may be NULL) stores and reuses the choice
  * per device and problem list. */
 kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream);
 kg_status kg_batch_set_config(kg_batch b, int shape, int ctas_per_sm);

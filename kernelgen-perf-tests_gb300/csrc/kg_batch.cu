@@ -27,6 +27,8 @@
 #include <string>
 #include <vector>
 
+#include <algorithm>
+
 #include "kg_engine.cuh"
 #include "kg_internal.h"
 
@@ -69,10 +71,60 @@ __device__ __forceinline__ void batch_roles(const BatchDesc& d, long long step, 
 	}
 }
 
+// One tile of a batch problem.  The (i, j) columns of the update domain are
+// numbered row by row and a tile takes NT consecutive ones (3D: each thread
+// then walks KC planes of its column; 2D: KC points NT apart), so tiles of
+// narrow problems are not cut at every row end: only the last tile of a
+// plane runs partly idle.
+template <class Op, class N, class S, int NT, int KC, int UK>
+__device__ __forceinline__ void sweep_lin(const Op& op, const Ptrs<S>& p, int nx, int ny, int ns, int tcol, int tz)
+{
+	constexpr Slots sl = Op::slots();
+	constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
+	const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+	const int dxn = nx - Op::LX - Op::HX, dyn = ny - Op::LY - Op::HY;
+	const long long ncol = (long long)dxn * dyn;
+	const long long sy = nx, sz = (long long)nx * ny;
+	if (k2d) {
+#pragma unroll 1
+		for (int r = 0; r < KC; r++) {
+			const long long col = ((long long)tcol * KC + r) * NT + tid;
+			if (col >= ncol) break;
+			const int j = Op::LY + (int)(col / dxn), i = Op::LX + (int)(col - (col / dxn) * dxn);
+			const long long c = i + sy * j;
+			GAcc<N, S> at{p.in, c, sy, sz};
+			N o[3];
+			op.point(at, o);
+#pragma unroll
+			for (int q = 0; q < sl.nout; q++) p.out[q][c] = Conv<N, S>::to(o[q]);
+		}
+	} else {
+		const long long col = (long long)tcol * NT + tid;
+		if (col >= ncol) return;
+		const int j = Op::LY + (int)(col / dxn), i = Op::LX + (int)(col - (col / dxn) * dxn);
+		const int k0 = Op::LZ + tz * KC, k1 = min(k0 + KC, ns - Op::HZ);
+#pragma unroll UK
+		for (int k = k0; k < k1; k++) {
+			const long long c = i + sy * j + sz * k;
+			GAcc<N, S> at{p.in, c, sy, sz};
+			N o[3];
+			op.point(at, o);
+#pragma unroll
+			for (int q = 0; q < sl.nout; q++) p.out[q][c] = Conv<N, S>::to(o[q]);
+		}
+	}
+}
+
+// Registers capped for 2048 resident threads per SM (32 per thread; a few
+// spill): the batch's small tiles are bound by load latency, and the extra
+// warps hide it.  Measured on 256 FP32 problems (Gpts/s, best tile shape and
+// CTAs per SM): 188 uncapped (40 registers, 6 CTAs of 256 threads), 282
+// capped.
 template <class N, class S, int BX, int BY, int KC>
-__global__ void __launch_bounds__(BX * BY) batch_kernel(const BatchDesc* __restrict__ desc, int nprob,
+__global__ void __launch_bounds__(BX * BY, 2048 / (BX * BY)) batch_kernel(const BatchDesc* __restrict__ desc, int nprob,
 	int total, const long long* __restrict__ step_base, int local)
 {
+	constexpr int NT = BX * BY;
 	__shared__ int first[kBatchMax + 1];
 	for (int q = threadIdx.x + threadIdx.y * BX; q < nprob; q += BX * BY) first[q] = desc[q].first;
 	__syncthreads();
@@ -85,28 +137,25 @@ __global__ void __launch_bounds__(BX * BY) batch_kernel(const BatchDesc* __restr
 			else hi = mid - 1;
 		}
 		const BatchDesc& d = desc[lo];
-		int t = item - d.first;
-		const int tx = t % d.tiles_x;
-		t /= d.tiles_x;
-		const int ty = t % d.tiles_y;
-		const int tz = t / d.tiles_y;
+		const int t = item - d.first;
+		const int tcol = t % d.tiles_x, tz = t / d.tiles_x;
 		Ptrs<S> p{};
 		batch_roles<S>(d, step, p);
 		switch (d.stencil) {
 		case KG_LAPLACIAN:
-			sweep_tile<OpLaplacian<N>, N, S, BX, BY, KC, 4>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, p, d.nx, d.ny, d.ns, tx, ty, tz);
+			sweep_lin<OpLaplacian<N>, N, S, NT, KC, 4>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, p, d.nx, d.ny, d.ns, tcol, tz);
 			break;
 		case KG_DIVERGENCE:
-			sweep_tile<OpDivergence<N>, N, S, BX, BY, KC, 4>(OpDivergence<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])},
-				p, d.nx, d.ny, d.ns, tx, ty, tz);
+			sweep_lin<OpDivergence<N>, N, S, NT, KC, 4>(OpDivergence<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])},
+				p, d.nx, d.ny, d.ns, tcol, tz);
 			break;
 		case KG_WAVE13PT:
-			sweep_tile<OpWave13pt<N>, N, S, BX, BY, KC, 4>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])},
-				p, d.nx, d.ny, d.ns, tx, ty, tz);
+			sweep_lin<OpWave13pt<N>, N, S, NT, KC, 4>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])},
+				p, d.nx, d.ny, d.ns, tcol, tz);
 			break;
 		case KG_GAUSSBLUR:
-			sweep_tile<OpGaussblur<N>, N, S, BX, BY, KC, 4>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]),
-				N(d.c[3]), N(d.c[4]), N(d.c[5]), N(d.c[6])}, p, d.nx, d.ny, d.ns, tx, ty, tz);
+			sweep_lin<OpGaussblur<N>, N, S, NT, KC, 4>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]),
+				N(d.c[3]), N(d.c[4]), N(d.c[5]), N(d.c[6])}, p, d.nx, d.ny, d.ns, tcol, tz);
 			break;
 		default: break;
 		}
@@ -120,10 +169,9 @@ __global__ void batch_advance(long long* step_base, int n)
 
 // Tile shapes the tuner tries (BX, BY, KC).
 struct Shape { int bx, by, kc; };
-static const Shape k_shapes[] = {{32, 8, 8}, {32, 4, 8}, {64, 4, 8}, {32, 8, 4}, {32, 8, 16}, {128, 2, 8}};
+static const Shape k_shapes[] = {{32, 8, 8}, {32, 4, 8}, {64, 4, 8}, {32, 8, 4}, {32, 8, 16}, {128, 2, 8},
+	{32, 8, 32}, {32, 16, 16}, {32, 4, 32}, {32, 8, 64}};
 static const int k_nshapes = sizeof(k_shapes) / sizeof(k_shapes[0]);
-static const int k_ctas[] = {2, 4, 8};
-static const int k_nctas = sizeof(k_ctas) / sizeof(k_ctas[0]);
 
 template <class N, class S>
 static cudaError_t launch_shape(int shape, dim3 grid, const BatchDesc* desc, int nprob, int total,
@@ -138,26 +186,63 @@ static cudaError_t launch_shape(int shape, dim3 grid, const BatchDesc* desc, int
 	KG_SHAPE_CASE(3, 32, 8, 4)
 	KG_SHAPE_CASE(4, 32, 8, 16)
 	KG_SHAPE_CASE(5, 128, 2, 8)
+	KG_SHAPE_CASE(6, 32, 8, 32)
+	KG_SHAPE_CASE(7, 32, 16, 16)
+	KG_SHAPE_CASE(8, 32, 4, 32)
+	KG_SHAPE_CASE(9, 32, 8, 64)
 #undef KG_SHAPE_CASE
 	default: return cudaErrorInvalidValue;
 	}
 	return cudaGetLastError();
 }
 
+// Tiles of one problem for a shape: runs of bx*by columns (3D: times runs
+// of kc planes; 2D: kc runs per tile).
+// Resident CTAs per SM of the kernel of a shape (the persistent grid should
+// not exceed one wave: a CTA that starts late runs its share of the items
+// after the others have finished).
+template <class N, class S>
+static int shape_occupancy(int shape)
+{
+	int n = 0;
+	switch (shape) {
+#define KG_OCC_CASE(I, BX, BY, KC) \
+	case I: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<N, S, BX, BY, KC>, BX * BY, 0); break;
+	KG_OCC_CASE(0, 32, 8, 8)
+	KG_OCC_CASE(1, 32, 4, 8)
+	KG_OCC_CASE(2, 64, 4, 8)
+	KG_OCC_CASE(3, 32, 8, 4)
+	KG_OCC_CASE(4, 32, 8, 16)
+	KG_OCC_CASE(5, 128, 2, 8)
+	KG_OCC_CASE(6, 32, 8, 32)
+	KG_OCC_CASE(7, 32, 16, 16)
+	KG_OCC_CASE(8, 32, 4, 32)
+	KG_OCC_CASE(9, 32, 8, 64)
+#undef KG_OCC_CASE
+	default: break;
+	}
+	return n > 0 ? n : 1;
+}
+
 static int tiles_of(int stencil, int nx, int ny, int ns, const Shape& s, int* tx, int* ty, int* tz)
 {
-	auto set = [&](auto tc) {
-		using T = decltype(tc);
-		*tx = T::x(nx, s.bx);
-		*ty = T::y(ny, s.by, s.kc);
-		*tz = T::z(ns, s.kc);
-	};
+	int lx, hx, ly, hy, lz, hz;
 	switch (stencil) {
-	case KG_LAPLACIAN: set(TileCount<OpLaplacian<FF>>{}); break;
-	case KG_DIVERGENCE: set(TileCount<OpDivergence<FF>>{}); break;
-	case KG_WAVE13PT: set(TileCount<OpWave13pt<FF>>{}); break;
-	case KG_GAUSSBLUR: set(TileCount<OpGaussblur<FF>>{}); break;
+	case KG_LAPLACIAN: case KG_DIVERGENCE: lx = hx = ly = hy = lz = hz = 1; break;
+	case KG_WAVE13PT: lx = hx = ly = hy = lz = hz = 2; break;
+	case KG_GAUSSBLUR: lx = hx = ly = hy = 2; lz = hz = 0; break;
 	default: return -1;
+	}
+	const long long nt = (long long)s.bx * s.by;
+	const long long ncol = (long long)std::max(0, nx - lx - hx) * std::max(0, ny - ly - hy);
+	const int dz = std::max(0, ns - lz - hz);
+	*ty = 1;
+	if (lz == 0 && hz == 0) {
+		*tx = (int)((ncol + nt * s.kc - 1) / (nt * s.kc));
+		*tz = ncol > 0 ? 1 : 0;
+	} else {
+		*tx = (int)((ncol + nt - 1) / nt);
+		*tz = (dz + s.kc - 1) / s.kc;
 	}
 	return 0;
 }
@@ -392,8 +477,12 @@ kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream)
 	// Each trial advances the batch; the roles stay consistent because the
 	// device step counter advances with them.
 	for (int sh = 0; sh < k_nshapes && s == KG_OK; sh++) {
-		for (int c = 0; c < k_nctas && s == KG_OK; c++) {
-			if ((s = kg_batch_set_config(b, sh, k_ctas[c])) != KG_OK) break;
+		// one wave of resident CTAs, one fewer per SM, half as many
+		const int occ = b->dtype == KG_F32 ? shape_occupancy<FF, float>(sh) : shape_occupancy<SD, double>(sh);
+		int cand[3] = {occ, occ > 1 ? occ - 1 : 1, occ > 1 ? occ / 2 : 1};
+		for (int c = 0; c < 3 && s == KG_OK; c++) {
+			if (c > 0 && (cand[c] == cand[c - 1] || (c == 2 && cand[2] == cand[0]))) continue;
+			if ((s = kg_batch_set_config(b, sh, cand[c])) != KG_OK) break;
 			if ((s = kg_batch_step(b, 1, stream)) != KG_OK) break;  // warm-up
 			cudaEventRecord(e0, st);
 			if ((s = kg_batch_step(b, 3, stream)) != KG_OK) break;
@@ -401,7 +490,7 @@ kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream)
 			if ((s = fail_cuda(cudaEventSynchronize(e1), "kg_batch_tune")) != KG_OK) break;
 			float ms = 0;
 			cudaEventElapsedTime(&ms, e0, e1);
-			if (ms < best) { best = ms; best_shape = sh; best_ctas = k_ctas[c]; }
+			if (ms < best) { best = ms; best_shape = sh; best_ctas = cand[c]; }
 		}
 	}
 	cudaEventDestroy(e0);
