@@ -8,13 +8,16 @@
 //                           copies, own column in registers.
 // Strict and contracted FP64 (SD, FD) are bound by the FP64 pipe and run
 // direct by default; FP32 arithmetic (FF) is bound by memory and runs on the
-// TMA engine for the stencils where that measured faster on GB300 (FP32,
-// 512x256x256 and 1024x512x512, Gpts/s direct -> TMA: laplacian 443 -> 493,
-// divergence 343 -> 382, gradient 238 -> 328, uxx1 170 -> 213, lapgsrb 260 ->
-// 268, BF16 uxx1 162 -> 245), where the arrays allow it, and direct for the
-// rest (wave13pt 341 vs 277, tricubic 95 vs 93, the 2D stencils);
-// float-float (FF2) is bound by issue slots and runs staged, which splits each
-// value once instead of once per use.
+// TMA engine for the stencils where that measured faster on GB300, where the
+// arrays allow it, and direct for the rest.  Same-run Gpts/s, direct -> TMA,
+// FP32 512x256x256: laplacian 443 -> 583, divergence 343 -> 402, gradient
+// 238 -> 325, uxx1 171 -> 224, lapgsrb 260 -> 289, wave13pt 340 -> 344,
+// tricubic 95 -> 86; 1024x512x512: laplacian 443 -> 681, uxx1 170 -> 234,
+// wave13pt 351 -> 377; BF16 1024x512x512: laplacian 482 -> 636, uxx1 162 ->
+// 264, wave13pt 354 -> 341.  tricubic, tricubic2 and the 2D stencils stay
+// direct, and wave13pt takes TMA for 4-byte storage only.  Float-float (FF2)
+// is bound by issue slots and runs staged, which splits each value once
+// instead of once per use.
 #pragma once
 
 #include <type_traits>
@@ -39,23 +42,23 @@ template <class N> struct Engines {
 	static constexpr int automatic = ff2 ? KG_ENGINE_STAGED : ff ? KG_ENGINE_TMA : KG_ENGINE_DIRECT;
 };
 
-inline bool tma_preferred(int stencil)
+inline bool tma_preferred(int stencil, int elem_bytes)
 {
 	return stencil == KG_LAPLACIAN || stencil == KG_DIVERGENCE || stencil == KG_GRADIENT ||
-		stencil == KG_UXX1 || stencil == KG_LAPGSRB;
+		stencil == KG_UXX1 || stencil == KG_LAPGSRB || (stencil == KG_WAVE13PT && elem_bytes == 4);
 }
 
-template <class N> int automatic_engine(int stencil)
+template <class N, class S> int automatic_engine(int stencil)
 {
 	const int e = Engines<N>::automatic;
-	return e == KG_ENGINE_TMA && !tma_preferred(stencil) ? KG_ENGINE_DIRECT : e;
+	return e == KG_ENGINE_TMA && !tma_preferred(stencil, (int)sizeof(S)) ? KG_ENGINE_DIRECT : e;
 }
 
 template <class Op, class N, class S>
 int resolve_engine(const kg_problem& pr)
 {
 	if (pr.engine != KG_ENGINE_AUTO) return pr.engine;
-	const int e = automatic_engine<N>(pr.stencil);
+	const int e = automatic_engine<N, S>(pr.stencil);
 	if (e == KG_ENGINE_TMA && !TmaLaunch<Op, N, S>::usable(pr)) return KG_ENGINE_DIRECT;
 	return e;
 }
@@ -84,7 +87,7 @@ cudaError_t regs_typed(const kg_problem& pr, int* nregs)
 	return with_op<N>(pr, [&](const auto& op) -> cudaError_t {
 		using Op = std::decay_t<decltype(op)>;
 		const void* f = nullptr;
-		const int e = automatic_engine<N>(pr.stencil);
+		const int e = automatic_engine<N, S>(pr.stencil);
 		if constexpr (Engines<N>::tma)
 			if (e == KG_ENGINE_TMA) f = TmaLaunch<Op, N, S>::func();
 		if constexpr (Engines<N>::staged)

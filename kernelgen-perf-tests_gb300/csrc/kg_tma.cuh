@@ -284,13 +284,31 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 	// ---- compute warps ----
 	const int tx = tid % TX, ty = tid / TX;
 	const int i = xt + tx;
-	const bool col_ok = i >= Op::LX && i < nx - Op::HX;
 	const long long sy = nx, sz = (long long)nx * ny;
+	// per point of this thread: byte offset inside a plane of each input, and
+	// whether it lies in the update domain (both fixed for the whole kernel)
+	int toff[PY][6];
+	bool pt_ok[PY];
+#pragma unroll
+	for (int r = 0; r < PY; r++) {
+		const int j = yt + ty + r * TY;
+		pt_ok[r] = i >= Op::LX && i < nx - Op::HX && j < ny - Op::HY;
+#pragma unroll
+		for (int q = 0; q < G::NIN; q++)
+			toff[r][q] = ((ty + r * TY + Op::halo(q).y0) * G::W(q) + tx + G::XL(q)) * G::ES;
+	}
 	uint32_t g = 0;
 	for (int kb = Op::LZ + blockIdx.z * kc; kb < kend; kb += gridDim.z * kc) {
 		const int nsteps = min(kc, kend - kb);
 		M col[PY][6][ZMAX];
 		int sb[6];
+		// this thread's outputs at plane kb; each step moves them one plane on
+		S* outp[PY][3];
+#pragma unroll
+		for (int r = 0; r < PY; r++)
+#pragma unroll
+			for (int q = 0; q < sl.nout; q++)
+				outp[r][q] = p.out[q] + (i + sy * (yt + ty + r * TY) + sz * kb);
 		for (int s = 0; s < nsteps; s++) {
 			const int k = kb + s;
 			const uint32_t gs = g + s;
@@ -304,17 +322,14 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 			}
 #pragma unroll
 			for (int r = 0; r < PY; r++) {
-				const int j = yt + ty + r * TY;
-				int toff[6];
 #pragma unroll
 				for (int q = 0; q < G::NIN; q++) {
 					const Halo h = Op::halo(q);
-					toff[q] = ((ty + r * TY + h.y0) * G::W(q) + tx + G::XL(q)) * G::ES;
 					// own column: shift by one plane and read the newest (all of
 					// them at the first step of a run)
 					const int nz = G::NZ(q);
 					if (G::staged(q) && nz > 1) {
-						const unsigned char* ring = sm + G::offset(q) + toff[q];
+						const unsigned char* ring = sm + G::offset(q) + toff[r][q];
 						if (s == 0) {
 #pragma unroll
 							for (int m = 0; m < ZMAX; m++)
@@ -330,14 +345,16 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 						}
 					}
 				}
-				if (col_ok && j < ny - Op::HY) {
-					const long long c = i + sy * j + sz * k;
-					TAcc<Op, N, S, G, ZMAX> at{sm, toff, sb, col[r], p.in, c, sy, sz};
+				if (pt_ok[r]) {
+					const long long c = i + sy * (yt + ty + r * TY) + sz * k;
+					TAcc<Op, N, S, G, ZMAX> at{sm, toff[r], sb, col[r], p.in, c, sy, sz};
 					N o[3];
 					op.point(at, o);
 #pragma unroll
-					for (int q = 0; q < sl.nout; q++) p.out[q][c] = Conv<N, S>::to(o[q]);
+					for (int q = 0; q < sl.nout; q++) *outp[r][q] = Conv<N, S>::to(o[q]);
 				}
+#pragma unroll
+				for (int q = 0; q < sl.nout; q++) outp[r][q] += sz;
 			}
 			// this warp is done with the step's planes
 			__syncwarp();
