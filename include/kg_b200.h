@@ -263,11 +263,19 @@ kg_status kg_program_run(kg_problem* p, int nt, int copy_back_mask, kg_timings* 
 /* ---- launch plans: the nt-sweep loop captured as one CUDA graph ---------- */
 
 typedef struct kg_plan_s* kg_plan;
-/* Records nt sweeps of p (device pointers) with the reference's rotation. */
+/* Records nt sweeps of p (device pointers) with the reference's rotation.
+ * tricubic and tricubic2 in KG_F64 / KG_F64_FMA: the plan also owns 64
+ * weight planes (512 bytes per point, taken when they leave half of the free
+ * device memory free): each replay first evaluates the loop-invariant weight
+ * products of every point once (a, b, c do not change during the loop) and
+ * the nt sweeps read them; results are bit for bit those of nt kg_sweep
+ * calls.  kg_program_run does the same with the planes from its pool. */
 kg_status kg_plan_create(kg_plan* plan, const kg_problem* p, int nt);
 kg_status kg_plan_launch(kg_plan plan, kg_stream_t stream);
 /* After a launch: p->arr in their final roles. */
 kg_status kg_plan_final_roles(kg_plan plan, kg_problem* p);
+/* Kernel launches in one replay of the plan (-1 on a bad plan). */
+int kg_plan_kernels(kg_plan plan);
 kg_status kg_plan_destroy(kg_plan plan);
 
 /* ---- batches: many uneven problems, one persistent launch per step ------ */

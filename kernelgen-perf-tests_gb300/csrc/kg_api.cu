@@ -128,6 +128,8 @@ static cudaError_t dispatch(const kg_problem& p, cudaStream_t st)
 	}
 }
 
+kg_status validate_problem(const kg_problem* p) { return validate(p); }
+
 kg_status sweep_checked(const kg_problem* p, cudaStream_t st)
 {
 	kg_status s = validate(p);

@@ -31,4 +31,9 @@ void clear_error();
 
 size_t dtype_size(int dt);
 
+// Tricubic programs with loop-invariant weights (kg_tricubic_pw.cu).
+size_t tricubic_pw_bytes(const kg_problem& p);
+cudaError_t tricubic_pw_precompute(const kg_problem& p, double* pw, cudaStream_t st);
+cudaError_t tricubic_pw_sweep(const kg_problem& p, const double* pw, cudaStream_t st);
+
 }  // namespace kg

@@ -10,6 +10,7 @@
 
 namespace kg {
 kg_status sweep_checked(const kg_problem* p, cudaStream_t st);
+kg_status validate_problem(const kg_problem* p);
 const char* stencil_name(int s);
 
 // Pointer rotation after one sweep, as the reference loops do it:
@@ -36,8 +37,9 @@ static double now_s()
 // by the library.  Allocating and freeing on the stream keeps programs that
 // run concurrently on different streams from waiting on each other (cudaFree
 // waits for the whole device); up to kPoolKeep bytes stay cached between
-// calls, the rest goes back to the device when a stream synchronises.
-constexpr uint64_t kPoolKeep = 8ull << 30;
+// calls (room for two concurrent tricubic programs of 512x256x256 with their
+// weight planes), the rest goes back to the device when a stream synchronises.
+constexpr uint64_t kPoolKeep = 48ull << 30;
 
 static cudaError_t program_pool(cudaMemPool_t* out)
 {
@@ -76,7 +78,20 @@ struct kg_plan_s {
 	int perm[6];   // final role q is held by original array perm[q]
 	cudaGraph_t graph;
 	cudaGraphExec_t exec;
+	double* pw;    // tricubic: the loop-invariant weight planes (owned)
 };
+
+namespace kg {
+// Whether a tricubic program takes the precomputed-weight path: the planes
+// must leave at least half of the free device memory free.
+static bool pw_fits(size_t bytes)
+{
+	if (!bytes) return false;
+	size_t fr = 0, tot = 0;
+	if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); return false; }
+	return bytes <= fr / 2;
+}
+}  // namespace kg
 
 extern "C" {
 
@@ -128,9 +143,20 @@ kg_status kg_program_run(kg_problem* p, int nt, int copy_back_mask, kg_timings* 
 			s = fail_cuda(cudaMemcpyAsync(dev[q], p->arr[q], bytes, cudaMemcpyHostToDevice, st), "kg_program_run: load");
 		cudaEventRecord(*load1, st);
 	}
+	// tricubic: the loop-invariant weight planes once (part of the compute
+	// phase), then sweeps that read them
+	double* pw = nullptr;
+	if (s == KG_OK && nt > 0 && (s = validate_problem(&d)) == KG_OK && pw_fits(tricubic_pw_bytes(d))) {
+		if (cudaMallocFromPoolAsync((void**)&pw, tricubic_pw_bytes(d), pool, st) != cudaSuccess) {
+			cudaGetLastError();
+			pw = nullptr;
+		}
+		if (pw) s = fail_cuda(tricubic_pw_precompute(d, pw, st), "kg_program_run: tricubic weights");
+	}
 	for (int it = 0; it < nt && s == KG_OK; it++) {
 		cudaEventRecord(sweep[2 * it], st);
-		if ((s = sweep_checked(&d, st)) != KG_OK) break;
+		if ((s = pw ? fail_cuda(tricubic_pw_sweep(d, pw, st), "kg_program_run: tricubic")
+		            : sweep_checked(&d, st)) != KG_OK) break;
 		cudaEventRecord(sweep[2 * it + 1], st);
 		rotate_roles(p->stencil, d.arr);
 		rotate_roles(p->stencil, p->arr);
@@ -144,6 +170,7 @@ kg_status kg_program_run(kg_problem* p, int nt, int copy_back_mask, kg_timings* 
 		}
 		cudaEventRecord(*save1, st);
 	}
+	if (pw) cudaFreeAsync(pw, st);
 	for (int q = 0; q < narr; q++)
 		if (dev[q]) cudaFreeAsync(dev[q], st);
 	if (made == nev) cudaEventRecord(*free1, st);
@@ -191,10 +218,19 @@ kg_status kg_plan_create(kg_plan* plan, const kg_problem* p, int nt)
 	kg_status s = fail_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "kg_plan_create");
 	if (s != KG_OK) { delete pl; return s; }
 	kg_problem d = *p;
-	s = fail_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "kg_plan_create: capture");
+	// tricubic: the weight planes once, then nt sweeps that read them
+	if ((s = validate_problem(p)) == KG_OK && pw_fits(tricubic_pw_bytes(*p))) {
+		if (cudaMalloc((void**)&pl->pw, tricubic_pw_bytes(*p)) != cudaSuccess) {
+			cudaGetLastError();
+			pl->pw = nullptr;
+		}
+	}
+	if (s == KG_OK) s = fail_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "kg_plan_create: capture");
 	if (s == KG_OK) {
+		if (pl->pw) s = fail_cuda(tricubic_pw_precompute(d, pl->pw, cs), "kg_plan_create: tricubic weights");
 		for (int it = 0; it < nt && s == KG_OK; it++) {
-			s = sweep_checked(&d, cs);
+			s = pl->pw ? fail_cuda(tricubic_pw_sweep(d, pl->pw, cs), "kg_plan_create: tricubic")
+			           : sweep_checked(&d, cs);
 			rotate_roles(p->stencil, d.arr);
 			rotate_roles(p->stencil, pl->perm);
 		}
@@ -212,6 +248,7 @@ kg_status kg_plan_create(kg_plan* plan, const kg_problem* p, int nt)
 	if (s != KG_OK) {
 		if (pl->exec) cudaGraphExecDestroy(pl->exec);
 		if (pl->graph) cudaGraphDestroy(pl->graph);
+		if (pl->pw) cudaFree(pl->pw);
 		delete pl;
 		return s;
 	}
@@ -235,12 +272,30 @@ kg_status kg_plan_final_roles(kg_plan plan, kg_problem* p)
 	return KG_OK;
 }
 
+int kg_plan_kernels(kg_plan plan)
+{
+	if (!plan || !plan->graph) return -1;
+	size_t n = 0;
+	if (cudaGraphGetNodes(plan->graph, nullptr, &n) != cudaSuccess) return -1;
+	cudaGraphNode_t* nodes = new (std::nothrow) cudaGraphNode_t[n ? n : 1];
+	if (!nodes) return -1;
+	int k = 0;
+	if (cudaGraphGetNodes(plan->graph, nodes, &n) == cudaSuccess)
+		for (size_t i = 0; i < n; i++) {
+			cudaGraphNodeType t;
+			if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+		}
+	delete[] nodes;
+	return k;
+}
+
 kg_status kg_plan_destroy(kg_plan plan)
 {
 	clear_error();
 	if (!plan) return KG_OK;
 	if (plan->exec) cudaGraphExecDestroy(plan->exec);
 	if (plan->graph) cudaGraphDestroy(plan->graph);
+	if (plan->pw) cudaFree(plan->pw);
 	delete plan;
 	return KG_OK;
 }

@@ -39,6 +39,7 @@ EXPORTS = [
     "kg_batch_set_config", "kg_batch_get_config", "kg_batch_set_step", "kg_batch_final_roles",
     "kg_batch_destroy", "kg_poisson_solve", "kg_engine_status",
     "kg_vecadd", "kg_matvec", "kg_matmul", "kg_sincos", "kg_whispering", "kg_extra_regcount",
+    "kg_plan_kernels",
 ]
 EXTRA_TESTS = ["vecadd", "matvec", "matmul", "sincos", "whispering"]
 KG_ENGINE_AUTO, KG_ENGINE_DIRECT, KG_ENGINE_STAGED, KG_ENGINE_TMA = 0, 1, 2, 3
@@ -133,6 +134,7 @@ def _sig(lib):
         "kg_plan_launch": [P, P],
         "kg_plan_final_roles": [P, ctypes.POINTER(KgProblem)],
         "kg_plan_destroy": [P],
+        "kg_plan_kernels": [P],
         "kg_kernel_regcount": [I, I, ctypes.POINTER(I)],
         "kg_device_check": [],
         "kg_measure_peaks": [ctypes.POINTER(KgPeaks), P],
@@ -290,6 +292,10 @@ class Plan:
         p = KgProblem()
         check(load().kg_plan_final_roles(self.h, ctypes.byref(p)))
         return p
+
+    def kernels(self):
+        """Kernel launches in one replay."""
+        return load().kg_plan_kernels(self.h)
 
     def close(self):
         if self.h:

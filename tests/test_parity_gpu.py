@@ -324,3 +324,32 @@ def test_b200_driver_gameoflife_bernoulli_u8():
     assert "final mean = %f" % live in out
 
 
+
+
+@pytest.mark.parametrize("name", ["tricubic", "tricubic2"])
+@pytest.mark.parametrize("shape", [(5, 5, 5), (40, 33, 21), (129, 35, 20)])
+def test_tricubic_plan_precomputed_weights(name, shape):
+    """Plans of tricubic programs evaluate the loop-invariant weight products
+    once per replay (one extra kernel) and sweep from them: bit for bit the
+    oracle over two replays of four sweeps (an even count returns the roles,
+    so the second replay continues the first); the FMA form stays within
+    1e-12 of it."""
+    for dt in (kgb200.KG_F64, kgb200.KG_F64_FMA):
+        case = ol.Case(name, shape)
+        bufs = [torch.from_numpy(a).cuda() for a in case.arrays()]
+        p = kgb200.problem(name, dt, case.shape, case.coef, [b.data_ptr() for b in bufs])
+        plan = kgb200.Plan(p, 4)
+        assert plan.kernels() == 5
+        plan.launch()
+        plan.launch()
+        torch.cuda.synchronize()
+        fin = plan.final_roles()
+        plan.close()
+        case.run(8)
+        by = {b.data_ptr(): b for b in bufs}
+        for q, w in enumerate(case.arrays()):
+            g = by[fin.arr[q]].cpu().numpy()
+            if dt == kgb200.KG_F64:
+                assert np.array_equal(g.view(np.uint64), w.view(np.uint64)), (name, shape, q)
+            else:
+                assert normwise(g, w) <= 1e-12, (name, shape, q)
