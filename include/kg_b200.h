@@ -253,7 +253,7 @@ typedef struct {
  * free.  On return p->arr holds the host arrays in their final roles, as the
  * reference's idxs[] leaves them.  timings may be NULL.
  * Every phase is ordered on `stream` (device memory from a library-owned
- * stream-ordered pool that keeps up to 8 GiB cached between calls) and the
+ * stream-ordered pool that keeps up to 48 GiB cached between calls) and the
  * call waits for the stream once, at the end; so calls from different host
  * threads on different streams overlap one program's copies with another's
  * sweeps.  The host arrays should be pinned for the copies to overlap. */
