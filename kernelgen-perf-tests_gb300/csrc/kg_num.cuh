@@ -190,11 +190,14 @@ __device__ __forceinline__ FF2 operator*(FF2 a, FF2 b)
 	e = __fmaf_rn(a.lo, b.hi, e);
 	return ff2_fast_two_sum(p, e);
 }
+// Quotient: q1 ~ a.hi / b.hi (fast approximate FP32 division, ~2 ulp), the
+// remainder a - b q1 in float-float, and its quotient q2 as the correction;
+// q1 + q2 is within ~2^-44 of a / b.
 __device__ __forceinline__ FF2 operator/(FF2 a, FF2 b)
 {
-	const float q1 = __fdiv_rn(a.hi, b.hi);
+	const float q1 = __fdividef(a.hi, b.hi);
 	const FF2 r = a - b * FF2(q1, 0.f);
-	const float q2 = __fdiv_rn(r.hi, b.hi);
+	const float q2 = __fdividef(r.hi, b.hi);
 	return ff2_fast_two_sum(q1, q2);
 }
 

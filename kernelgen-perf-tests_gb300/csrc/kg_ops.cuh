@@ -116,7 +116,12 @@ template <class N> struct OpGradient {
 template <class N> struct OpUxx1 {
 	static constexpr int LX = 2, HX = 1, LY = 2, HY = 1, LZ = 2, HZ = 1;
 	static constexpr Slots slots() { return {{0, 2, 3, 4, 5}, 5, {1}, 1}; }
-	static constexpr Halo halo(int q) { constexpr Halo h[] = {{0, 0, 0, 0, 0, 0}, {0, 0, 1, 0, 1, 0}, {2, 1, 0, 0, 0, 0}, {0, 0, 2, 1, 0, 0}, {0, 0, 0, 0, 2, 1}}; return h[q]; }
+	// d1's reach; float-float reads d1 only through raw() (below), so the
+	// staged engines leave it in global memory
+	static constexpr Halo halo(int q) {
+		constexpr Halo h[] = {{0, 0, 0, 0, 0, 0}, {0, 0, 1, 0, 1, 0}, {2, 1, 0, 0, 0, 0}, {0, 0, 2, 1, 0, 0}, {0, 0, 0, 0, 2, 1}};
+		return (q == 1 && std::is_same<N, FF2>::value) ? Halo{0, 0, 0, 0, 0, 0} : h[q];
+	}
 	N c1, c2, dth;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int u0 = 0, d1 = 1, xx = 2, xy = 3, xz = 4;
@@ -134,12 +139,12 @@ template <class N> struct OpUxx1 {
 				at(d1, 0, 0, 0) + at(d1, 0, -1, 0) +
 				at(d1, 0, 0, -1) + at(d1, 0, -1, -1)));
 		}
-		o[0] = at(u0, 0, 0, 0) + pm(dth / d, (
-			pm(c1, at(xx, 0, 0, 0) - at(xx, -1, 0, 0)) +
-			pm(c2, at(xx, 1, 0, 0) - at(xx, -2, 0, 0)) +
-			pm(c1, at(xy, 0, 0, 0) - at(xy, 0, -1, 0)) +
-			pm(c2, at(xy, 0, 1, 0) - at(xy, 0, -2, 0)) +
-			pm(c1, at(xz, 0, 0, 0) - at(xz, 0, 0, -1)) +
+		o[0] = at(u0, 0, 0, 0) + pm(dth / d, nsum(
+			pm(c1, at(xx, 0, 0, 0) - at(xx, -1, 0, 0)),
+			pm(c2, at(xx, 1, 0, 0) - at(xx, -2, 0, 0)),
+			pm(c1, at(xy, 0, 0, 0) - at(xy, 0, -1, 0)),
+			pm(c2, at(xy, 0, 1, 0) - at(xy, 0, -2, 0)),
+			pm(c1, at(xz, 0, 0, 0) - at(xz, 0, 0, -1)),
 			pm(c2, at(xz, 0, 0, 1) - at(xz, 0, 0, -2))));
 	}
 };
