@@ -160,8 +160,8 @@ kg_status kg_extra_regcount(const char* name, kg_dtype dt, int* nregs);
 /* Which kernel design runs a sweep (kg_problem.engine).  AUTO: TMA for
  * KG_F32/KG_BF16/KG_F16 laplacian, divergence, gradient, uxx1 and lapgsrb
  * (and KG_F32 wave13pt) where every array and row starts on a 16-byte
- * boundary, else DIRECT;
- * DIRECT for KG_F64/KG_F64_FMA; STAGED for KG_F64_FF.  Built: DIRECT and TMA
+ * boundary, else DIRECT; DIRECT for KG_F64/KG_F64_FMA; STAGED for KG_F64_FF
+ * (TMA for its divergence and uxx1 where aligned).  Built: DIRECT and TMA
  * for every floating type but KG_F64_FF; STAGED and TMA for KG_F64_FF; DIRECT
  * for KG_U8.  The engines evaluate the same expressions in the same order (the
  * tests check their outputs equal bit for bit).  TMA needs 16-byte aligned

@@ -51,6 +51,12 @@ inline bool tma_preferred(int stencil, int elem_bytes)
 template <class N, class S> int automatic_engine(int stencil)
 {
 	const int e = Engines<N>::automatic;
+	// float-float: the staged engine splits each value once, which pays where
+	// values are used many times; divergence and uxx1 read most inputs along
+	// one axis only, and the TMA copies win there (FF2 Gpts/s at 512x256x256,
+	// staged -> TMA: divergence 88.6 -> 93.6, uxx1 45.2 -> 48.7; laplacian
+	// 130.8 -> 101.6, wave13pt 80.7 -> 62.7, tricubic 13.3 -> 6.6)
+	if (e == KG_ENGINE_STAGED) return (stencil == KG_DIVERGENCE || stencil == KG_UXX1) ? KG_ENGINE_TMA : e;
 	return e == KG_ENGINE_TMA && !tma_preferred(stencil, (int)sizeof(S)) ? KG_ENGINE_DIRECT : e;
 }
 
@@ -59,7 +65,8 @@ int resolve_engine(const kg_problem& pr)
 {
 	if (pr.engine != KG_ENGINE_AUTO) return pr.engine;
 	const int e = automatic_engine<N, S>(pr.stencil);
-	if (e == KG_ENGINE_TMA && !TmaLaunch<Op, N, S>::usable(pr)) return KG_ENGINE_DIRECT;
+	if (e == KG_ENGINE_TMA && !TmaLaunch<Op, N, S>::usable(pr))
+		return Engines<N>::ff2 ? KG_ENGINE_STAGED : KG_ENGINE_DIRECT;
 	return e;
 }
 
