@@ -85,36 +85,54 @@ cudaError_t vecadd_run(size_t n, const void* w0, const void* w1, void* w2, cudaS
 // ---- matvec/matvec.c:37-71: y[j] = 0; y[j] += A[i + nx j] * x[i], i = 0.. ----
 //
 // A CTA owns ROWS rows; column chunks of A (KC per row) and x go through
-// shared memory with coalesced loads, and each thread sums its row in order.
+// shared memory with coalesced loads, the next chunk's loads in flight in
+// registers while the current one is summed, and each thread sums its row in
+// order.  Strict FP64 forms the products on the integer pipes, so the FP64
+// unit only adds.
 
-constexpr int kMvRows = 128, kMvKC = 32;
+// 8 CTAs of 64 threads per SM (measured, 512 x 65536 strict FP64: 0.152 ms
+// with no register cap, 0.139 with this one, 0.181 with 12 CTAs; FP32 0.039,
+// 0.035, 0.033).
+constexpr int kMvRows = 64, kMvKC = 32, kMvMinBlocks = 8;
 
 template <class N, class S>
-__global__ void __launch_bounds__(kMvRows) matvec_kernel(int nx, int ny, const S* __restrict__ A,
+__global__ void __launch_bounds__(kMvRows, kMvMinBlocks) matvec_kernel(int nx, int ny, const S* __restrict__ A,
 	const S* __restrict__ x, S* __restrict__ y)
 {
 	__shared__ S tile[kMvRows][kMvKC + 1];
 	__shared__ S xs[kMvKC];
+	constexpr int PER = kMvKC;                 // elements per thread per chunk
 	const int t = threadIdx.x;
 	const int j0 = blockIdx.x * kMvRows, j = j0 + t;
-	N s = N(0.0);
-	for (int i0 = 0; i0 < nx; i0 += kMvKC) {
-		const int kc = min(kMvKC, nx - i0);
-#pragma unroll 4
-		for (int e = t; e < kMvRows * kMvKC; e += kMvRows) {
-			const int r = e / kMvKC, c = e - r * kMvKC;
-			if (j0 + r < ny && c < kc) tile[r][c] = __ldg(A + (size_t)(j0 + r) * nx + i0 + c);
+	S v[PER], xv{};
+	auto fetch = [&](int i0) {
+#pragma unroll
+		for (int q = 0; q < PER; q++) {
+			const int e = t + q * kMvRows, r = e / kMvKC, c = e - r * kMvKC;
+			v[q] = (j0 + r < ny && i0 + c < nx) ? __ldg(A + (size_t)(j0 + r) * nx + i0 + c) : S{};
 		}
-		if (t < kc) xs[t] = __ldg(x + i0 + t);
+		xv = (t < kMvKC && i0 + t < nx) ? __ldg(x + i0 + t) : S{};
+	};
+	N s = N(0.0);
+	if (nx > 0) fetch(0);
+	for (int i0 = 0; i0 < nx; i0 += kMvKC) {
+#pragma unroll
+		for (int q = 0; q < PER; q++) {
+			const int e = t + q * kMvRows, r = e / kMvKC, c = e - r * kMvKC;
+			tile[r][c] = v[q];
+		}
+		if (t < kMvKC) xs[t] = xv;
 		__syncthreads();
+		if (i0 + kMvKC < nx) fetch(i0 + kMvKC);
+		const int kc = min(kMvKC, nx - i0);
 		if (j < ny) {
 			if (kc == kMvKC) {
 #pragma unroll
 				for (int c = 0; c < kMvKC; c++)
-					s = s + mul_on(Conv<N, S>::from(tile[t][c]), Conv<N, S>::from(xs[c]), (c & 1) != 0);
+					s = s + mul_on(Conv<N, S>::from(tile[t][c]), Conv<N, S>::from(xs[c]), true);
 			} else {
 				for (int c = 0; c < kc; c++)
-					s = s + mul_on(Conv<N, S>::from(tile[t][c]), Conv<N, S>::from(xs[c]), (c & 1) != 0);
+					s = s + mul_on(Conv<N, S>::from(tile[t][c]), Conv<N, S>::from(xs[c]), true);
 			}
 		}
 		__syncthreads();
@@ -130,6 +148,10 @@ __global__ void __launch_bounds__(kMvRows) matvec_kernel(int nx, int ny, const S
 // memory, and every output accumulates its products in k order.
 
 constexpr int kMmTI = 32, kMmTJ = 32, kMmKC = 16;
+// Of each thread's four products per k, the first kMmInt on the integer
+// pipes (strict FP64; 512x256x256, ms: 2 of 4 0.131, 3 of 4 0.113, 4 of 4
+// 0.119).
+constexpr int kMmInt = 3;
 
 template <class N, class S>
 __global__ void __launch_bounds__(256) matmul_kernel(int nx, int ny, int ns, const S* __restrict__ A,
@@ -162,13 +184,13 @@ __global__ void __launch_bounds__(256) matmul_kernel(int nx, int ny, int ns, con
 			for (int kk = 0; kk < kMmKC; kk++) {
 				const N a = Conv<N, S>::from(As[kk][tx]);
 #pragma unroll
-				for (int m = 0; m < 4; m++) c[m] = c[m] + mul_on(a, Conv<N, S>::from(Bs[ty + 8 * m][kk]), m < 2);
+				for (int m = 0; m < 4; m++) c[m] = c[m] + mul_on(a, Conv<N, S>::from(Bs[ty + 8 * m][kk]), m < kMmInt);
 			}
 		} else {
 			for (int kk = 0; kk < kc; kk++) {
 				const N a = Conv<N, S>::from(As[kk][tx]);
 #pragma unroll
-				for (int m = 0; m < 4; m++) c[m] = c[m] + mul_on(a, Conv<N, S>::from(Bs[ty + 8 * m][kk]), m < 2);
+				for (int m = 0; m < 4; m++) c[m] = c[m] + mul_on(a, Conv<N, S>::from(Bs[ty + 8 * m][kk]), m < kMmInt);
 			}
 		}
 		__syncthreads();
