@@ -234,9 +234,10 @@ __global__ void __launch_bounds__(256) whispering_e_kernel(int nx, int ny, S* __
 	for (int j = 1 + blockIdx.y * 8 + threadIdx.y; j < ny - 1; j += gridDim.y * 8) {
 		const size_t c = i + (size_t)nx * j;
 		using Cv = Conv<N, S>;
+		auto M = [](N a, N b) { return mul_on(a, b, true); };
 		const N vca = Cv::ld(ca + c), vcb = Cv::ld(cb + c), vh = Cv::ld(h0 + c);
-		const N e0 = vca * Cv::from(e[c]) + vcb * (Cv::ld(h0 + c + nx) - vh);
-		const N e1 = vca * Cv::from(e[c + plane]) - vcb * (Cv::ld(h0 + c + 1) - vh);
+		const N e0 = M(vca, Cv::from(e[c])) + M(vcb, Cv::ld(h0 + c + nx) - vh);
+		const N e1 = M(vca, Cv::from(e[c + plane])) - M(vcb, Cv::ld(h0 + c + 1) - vh);
 		e[c] = Cv::to(e0);
 		e[c + plane] = Cv::to(e1);
 	}
@@ -254,13 +255,14 @@ __global__ void __launch_bounds__(256) whispering_h_kernel(int nx, int ny, N mu,
 	for (int j = 1 + blockIdx.y * 8 + threadIdx.y; j < ny - 1; j += gridDim.y * 8) {
 		const size_t c = i + (size_t)nx * j;
 		using Cv = Conv<N, S>;
+		auto M = [](N a, N b) { return mul_on(a, b, true); };
 		const N vh = Cv::ld(h0 + c);
 		const N e0 = Cv::ld(e + c), e1 = Cv::ld(e + c + plane);
-		const N ey = Cv::ld(ca + c - nx) * Cv::ld(e + c - nx) + Cv::ld(cb + c - nx) * (vh - Cv::ld(h0 + c - nx));
-		const N ex = Cv::ld(ca + c - 1) * Cv::ld(e + c - 1 + plane) - Cv::ld(cb + c - 1) * (vh - Cv::ld(h0 + c - 1));
-		const N h = Cv::ld(da + c) * vh + Cv::ld(db + c) * (e0 - ey + ex - e1);
+		const N ey = M(Cv::ld(ca + c - nx), Cv::ld(e + c - nx)) + M(Cv::ld(cb + c - nx), vh - Cv::ld(h0 + c - nx));
+		const N ex = M(Cv::ld(ca + c - 1), Cv::ld(e + c - 1 + plane)) - M(Cv::ld(cb + c - 1), vh - Cv::ld(h0 + c - 1));
+		const N h = M(Cv::ld(da + c), vh) + M(Cv::ld(db + c), e0 - ey + ex - e1);
 		h1[c] = Cv::to(h);
-		u_em1[c] = Cv::to(Cv::ld(u_em0 + c) + N(0.5) * (h * h / mu + epsilon * (e0 * e0 + e1 * e1)));
+		u_em1[c] = Cv::to(Cv::ld(u_em0 + c) + M(N(0.5), M(h, h) / mu + M(epsilon, M(e0, e0) + M(e1, e1))));
 	}
 }
 
