@@ -162,14 +162,18 @@ __global__ void __launch_bounds__(BX * BY) staged3d_kernel(Op op, Ptrs<S> p, int
 	M* sm = reinterpret_cast<M*>(smem_raw);
 
 	const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * BX + tx;
-	const int x0 = Op::LX + blockIdx.x * BX, y0 = Op::LY + blockIdx.y * BY;
-	const int i = x0 + tx, j = y0 + ty;
-	const bool mine = i < nx - Op::HX && j < ny - Op::HY;
+	const int x0 = Op::LX + blockIdx.x * BX;
+	const int i = x0 + tx;
 	const long long sy = nx, sz = (long long)nx * ny;
 	const int kend = ns - Op::HZ;
+	// rows of tiles beyond the grid's y limit (65535) are taken in turn
+	const int tyn = (ny - Op::LY - Op::HY + BY - 1) / BY;
 	Prefetch<Op, N, S, BX, BY> pf;
 
+	for (int yb = blockIdx.y; yb < tyn; yb += gridDim.y)
 	for (int kb = Op::LZ + blockIdx.z * KC; kb < kend; kb += gridDim.z * KC) {
+		const int y0 = Op::LY + yb * BY, j = y0 + ty;
+		const bool mine = i < nx - Op::HX && j < ny - Op::HY;
 		const int ke = min(kb + KC, kend);
 		// planes kb - z0 .. kb + z1 - 1 of each staged input: plane kk + z1
 		// of input q is the prefetch of step kk, so run steps kb-z0-z1 ..

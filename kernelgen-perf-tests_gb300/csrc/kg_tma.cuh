@@ -221,7 +221,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 // ahead of the compute warps, which never wait for each other.
 template <class Op, class N, class S, int TX, int TY, int PY, int L>
 __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, const __grid_constant__ TMaps maps,
-	int nx, int ny, int ns, int kc, int* err)
+	int nx, int ny, int ns, int kc, int yt0, int* err)
 {
 	constexpr int BX = TX, BY = TY * PY, NC = TX * TY;
 	using G = TGeo<Op, S, BX, BY, L>;
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 	uint64_t* done = full + NB;
 
 	const int tid = threadIdx.x;
-	const int xt = blockIdx.x * BX, yt = Op::LY + blockIdx.y * BY;
+	const int xt = blockIdx.x * BX, yt = Op::LY + (yt0 + (int)blockIdx.y) * BY;
 	const int kend = ns - Op::HZ;
 
 	if (tid == 0) {
@@ -416,11 +416,10 @@ struct TmaLaunch {
 	using G = TGeo<K, S, TX, TY * PY, L>;
 	static const void* func() { return (const void*)tma_kernel<K, N, S, TX, TY, PY, L>; }
 
-	// The copies need 16-byte aligned arrays and rows; y tiles index the grid.
+	// The copies need 16-byte aligned arrays and rows.
 	static bool usable(const kg_problem& pr) {
 		constexpr Slots sl = Op::slots();
 		if (((size_t)pr.nx * sizeof(S)) % 16) return false;
-		if (!k2d && (pr.ny - K::LY - K::HY + TY * PY - 1) / (TY * PY) > 65535) return false;
 		for (int q = 0; q < sl.nin; q++)
 			if ((uintptr_t)pr.arr[sl.in[q]] % 16) return false;
 		return true;
@@ -481,9 +480,13 @@ struct TmaLaunch {
 		K kop;
 		if constexpr (k2d) kop.op = op;
 		else kop = op;
-		dim3 grid(gx, (unsigned)min(gy, 65535), (unsigned)min(nz, 65535));
-		tma_kernel<K, N, S, TX, TY, PY, L><<<grid, threads, smem, st>>>(kop, p, maps, nx, ny, ns, kc, err);
-		return cudaGetLastError();
+		// y tiles beyond the grid's limit (65535) go to further launches
+		for (int y0 = 0; y0 < gy; y0 += 65535) {
+			dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
+			tma_kernel<K, N, S, TX, TY, PY, L><<<grid, threads, smem, st>>>(kop, p, maps, nx, ny, ns, kc, y0, err);
+			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+		}
+		return cudaSuccess;
 	}
 };
 
