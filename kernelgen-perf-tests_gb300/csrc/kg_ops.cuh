@@ -235,6 +235,48 @@ template <class N, bool FROM_ZERO> struct OpTricubicT {
 			o[0] = N(s);
 			return;
 		}
+		if constexpr (std::is_same<N, FF2>::value) {
+			// Float-float: the 16 products wa*wb once; per term the products
+			// *wc and *u0 as FMA error-free pairs left unnormalised (the next
+			// product takes the pair as it is), and the in-order sum as one
+			// chain of TwoSums whose errors collect, with the terms' low
+			// parts, in one FP32 accumulator renormalised at the end (as
+			// nsum): 16 FP32 operations per term instead of 25.
+			FF2 wab[16];
+#pragma unroll
+			for (int jj = 0; jj < 4; jj++)
+#pragma unroll
+				for (int ii = 0; ii < 4; ii++) wab[jj * 4 + ii] = wa[ii] * wb[jj];
+			float s = 0.f, e = 0.f;
+#pragma unroll
+			for (int kk = 0; kk < 4; kk++)
+#pragma unroll
+				for (int jj = 0; jj < 4; jj++)
+#pragma unroll
+					for (int ii = 0; ii < 4; ii++) {
+						const FF2 w = wab[jj * 4 + ii], c = wc[kk];
+						const FF2 u = at(u0, ii - 1, jj - 1, kk - 1);
+						const float p = __fmul_rn(w.hi, c.hi);
+						float pe = __fmaf_rn(w.hi, c.hi, -p);
+						pe = __fmaf_rn(w.hi, c.lo, pe);
+						pe = __fmaf_rn(w.lo, c.hi, pe);
+						const float t = __fmul_rn(p, u.hi);
+						float te = __fmaf_rn(p, u.hi, -t);
+						te = __fmaf_rn(p, u.lo, te);
+						te = __fmaf_rn(pe, u.hi, te);
+						if (kk == 0 && jj == 0 && ii == 0) {
+							s = t;
+							e = te;
+						} else {
+							const float n = __fadd_rn(s, t);
+							const float bb = __fsub_rn(n, s);
+							e = __fadd_rn(e, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(n, bb)), __fsub_rn(t, bb)), te));
+							s = n;
+						}
+					}
+			o[0] = ff2_fast_two_sum(s, e);
+			return;
+		}
 		N s;
 #pragma unroll
 		for (int kk = 0; kk < 4; kk++)
