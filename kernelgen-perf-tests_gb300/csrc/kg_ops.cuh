@@ -169,8 +169,34 @@ template <class N> struct OpWave13pt {
 	}
 };
 
-// tricubic/tricubic.c:1041-1054: cubic Lagrange weights, same association.
+// Float-float product left unnormalised: the pair (p, e) with p the FP32
+// product of the high parts and e its FMA error plus the cross terms.
+__device__ __forceinline__ FF2 ff2_mul_pair(FF2 a, FF2 b)
+{
+	const float p = __fmul_rn(a.hi, b.hi);
+	float e = __fmaf_rn(a.hi, b.hi, -p);
+	e = __fmaf_rn(a.hi, b.lo, e);
+	e = __fmaf_rn(a.lo, b.hi, e);
+	return FF2(p, e);
+}
+
+// tricubic/tricubic.c:1041-1054: cubic Lagrange weights, same association
+// (float-float: the same polynomials, operation order free within its bound).
 template <class N> __device__ __forceinline__ void tricubic_weights(N a, N* w) {
+	if constexpr (std::is_same<N, FF2>::value) {
+		// float-float: the three pairwise products shared by the four
+		// weights, unnormalised intermediates, +-1/2 applied exactly
+		const FF2 ap = a + FF2(1.f, 0.f), a2 = a + FF2(2.f, 0.f), am = a - FF2(1.f, 0.f);
+		const FF2 p1 = ff2_mul_pair(a, ap), p2 = ff2_mul_pair(am, a), p3 = ff2_mul_pair(am, ap);
+		const FF2 c6(1.0 / 6.0);
+		const FF2 h1 = ff2_mul_pair(p3, a2), h2 = ff2_mul_pair(p2, a2);
+		const FF2 g0 = ff2_mul_pair(c6, ff2_mul_pair(p1, a2)), g3 = ff2_mul_pair(c6, ff2_mul_pair(p2, ap));
+		w[0] = ff2_fast_two_sum(g0.hi, g0.lo);
+		w[1] = ff2_fast_two_sum(-0.5f * h1.hi, -0.5f * h1.lo);
+		w[2] = ff2_fast_two_sum(0.5f * h2.hi, 0.5f * h2.lo);
+		w[3] = ff2_fast_two_sum(-g3.hi, -g3.lo);
+		return;
+	}
 	const N one(1.0), two(2.0);
 	w[0] = N(1.0 / 6.0) * a * (a + one) * (a + two);
 	w[1] = N(-0.5) * (a - one) * (a + one) * (a + two);
@@ -236,45 +262,49 @@ template <class N, bool FROM_ZERO> struct OpTricubicT {
 			return;
 		}
 		if constexpr (std::is_same<N, FF2>::value) {
-			// Float-float: the 16 products wa*wb once; per term the products
-			// *wc and *u0 as FMA error-free pairs left unnormalised (the next
-			// product takes the pair as it is), and the in-order sum as one
-			// chain of TwoSums whose errors collect, with the terms' low
-			// parts, in one FP32 accumulator renormalised at the end (as
-			// nsum): 16 FP32 operations per term instead of 25.
+			// Float-float, a form whose operation order is free within its
+			// bound: s = sum_kk wc[kk] * (sum_jj,ii (wa[ii] wb[jj]) u0), each
+			// dot product accumulated as one chain of TwoSums whose errors
+			// collect, with the products' FMA error terms, in one FP32
+			// accumulator (as nsum), renormalised once per dot product; the
+			// products are left unnormalised (12 FP32 operations per term,
+			// and the 64 products wab * wc are not formed).
 			FF2 wab[16];
 #pragma unroll
 			for (int jj = 0; jj < 4; jj++)
 #pragma unroll
 				for (int ii = 0; ii < 4; ii++) wab[jj * 4 + ii] = wa[ii] * wb[jj];
-			float s = 0.f, e = 0.f;
+			auto chain = [](float& s, float& e, FF2 t) {
+				const float n = __fadd_rn(s, t.hi);
+				const float bb = __fsub_rn(n, s);
+				e = __fadd_rn(e, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(n, bb)), __fsub_rn(t.hi, bb)), t.lo));
+				s = n;
+			};
+			float S = 0.f, E = 0.f;
 #pragma unroll
-			for (int kk = 0; kk < 4; kk++)
+			for (int kk = 0; kk < 4; kk++) {
+				float s = 0.f, e = 0.f;
 #pragma unroll
 				for (int jj = 0; jj < 4; jj++)
 #pragma unroll
 					for (int ii = 0; ii < 4; ii++) {
-						const FF2 w = wab[jj * 4 + ii], c = wc[kk];
-						const FF2 u = at(u0, ii - 1, jj - 1, kk - 1);
-						const float p = __fmul_rn(w.hi, c.hi);
-						float pe = __fmaf_rn(w.hi, c.hi, -p);
-						pe = __fmaf_rn(w.hi, c.lo, pe);
-						pe = __fmaf_rn(w.lo, c.hi, pe);
-						const float t = __fmul_rn(p, u.hi);
-						float te = __fmaf_rn(p, u.hi, -t);
-						te = __fmaf_rn(p, u.lo, te);
-						te = __fmaf_rn(pe, u.hi, te);
-						if (kk == 0 && jj == 0 && ii == 0) {
-							s = t;
-							e = te;
+						const FF2 t = ff2_mul_pair(wab[jj * 4 + ii], at(u0, ii - 1, jj - 1, kk - 1));
+						if (jj == 0 && ii == 0) {
+							s = t.hi;
+							e = t.lo;
 						} else {
-							const float n = __fadd_rn(s, t);
-							const float bb = __fsub_rn(n, s);
-							e = __fadd_rn(e, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(n, bb)), __fsub_rn(t, bb)), te));
-							s = n;
+							chain(s, e, t);
 						}
 					}
-			o[0] = ff2_fast_two_sum(s, e);
+				const FF2 t = ff2_mul_pair(wc[kk], ff2_fast_two_sum(s, e));
+				if (kk == 0) {
+					S = t.hi;
+					E = t.lo;
+				} else {
+					chain(S, E, t);
+				}
+			}
+			o[0] = ff2_fast_two_sum(S, E);
 			return;
 		}
 		N s;
