@@ -152,7 +152,7 @@ __device__ __forceinline__ void commit_one(const Prefetch<Op, N, S, BX, BY>& pf,
 // Ring of planes along z, software-pipelined: while plane k is evaluated
 // from shared memory, the loads of plane k+1's new planes are in flight.
 template <class Op, class N, class S, int BX, int BY, int KC>
-__global__ void __launch_bounds__(BX * BY) staged3d_kernel(Op op, Ptrs<S> p, int nx, int ny, int ns)
+__device__ __forceinline__ void staged3d_body(const Op& op, const Ptrs<S>& p, int nx, int ny, int ns)
 {
 	using R = Rep<N, S>;
 	using M = typename R::M;
@@ -212,6 +212,28 @@ __global__ void __launch_bounds__(BX * BY) staged3d_kernel(Op op, Ptrs<S> p, int
 	}
 }
 
+template <class Op, class N, class S, int BX, int BY, int KC>
+__global__ void __launch_bounds__(BX * BY) staged3d_kernel(Op op, Ptrs<S> p, int nx, int ny, int ns)
+{
+	staged3d_body<Op, N, S, BX, BY, KC>(op, p, nx, ny, ns);
+}
+
+// The same kernel asked for at least four CTAs per SM (64 registers a
+// thread; ptxas then also schedules more independent work in flight), for
+// the ops where that measured faster (StagedOcc4).
+template <class Op, class N, class S, int BX, int BY, int KC>
+__global__ void __launch_bounds__(BX * BY, 4) staged3d_kernel_occ4(Op op, Ptrs<S> p, int nx, int ny, int ns)
+{
+	staged3d_body<Op, N, S, BX, BY, KC>(op, p, nx, ny, ns);
+}
+
+// Float-float tricubic, 512x256x256 on GB300: 1.71 -> 1.61 ms per sweep
+// with four CTAs per SM; every other stencil was slower with the cap
+// (laplacian 0.251 -> 0.281 ms, wave13pt 0.411 -> 0.482, gaussblur 0.476 ->
+// 0.514, ...).
+template <class Op> struct StagedOcc4 : std::false_type {};
+template <class N, bool Z> struct StagedOcc4<OpTricubicT<N, Z>> : std::true_type {};
+
 // A 2D op seen as a 3D op whose rows are planes: (dx, dy) -> (dx, 0, dy),
 // so the same plane-streaming kernel walks down the rows of a 2D grid with
 // a ring of rows, 256-point row segments per CTA.
@@ -240,7 +262,11 @@ struct StagedLaunch {
 	static constexpr int BX = k2d ? 256 : 32, BY = k2d ? 1 : 8, KC = k2d ? 64 : 16;
 	using M = typename Rep<N, S>::M;
 	static constexpr size_t smem() { return (size_t)Ring<K, BX, BY>::total() * sizeof(M); }
-	static const void* func() { return (const void*)staged3d_kernel<K, N, S, BX, BY, KC>; }
+	static constexpr bool occ4 = StagedOcc4<Op>::value;
+	static const void* func() {
+		if constexpr (occ4) return (const void*)staged3d_kernel_occ4<K, N, S, BX, BY, KC>;
+		else return (const void*)staged3d_kernel<K, N, S, BX, BY, KC>;
+	}
 	static cudaError_t run(const Op& op, const kg_problem& pr, cudaStream_t st) {
 		constexpr Slots sl = Op::slots();
 		Ptrs<S> p{};
@@ -265,7 +291,8 @@ struct StagedLaunch {
 		else kop = op;
 		dim3 block(BX, BY, 1);
 		dim3 grid((dx + BX - 1) / BX, (unsigned)min((dy + BY - 1) / BY, 65535), (unsigned)min((dz + KC - 1) / KC, 65535));
-		staged3d_kernel<K, N, S, BX, BY, KC><<<grid, block, bytes, st>>>(kop, p, nx, ny, ns);
+		if constexpr (occ4) staged3d_kernel_occ4<K, N, S, BX, BY, KC><<<grid, block, bytes, st>>>(kop, p, nx, ny, ns);
+		else staged3d_kernel<K, N, S, BX, BY, KC><<<grid, block, bytes, st>>>(kop, p, nx, ny, ns);
 		return cudaGetLastError();
 	}
 };
