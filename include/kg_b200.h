@@ -363,6 +363,23 @@ typedef struct {
 } kg_peaks;
 kg_status kg_measure_peaks(kg_peaks* out, kg_stream_t stream);
 
+/* Element-wise out[i] = a[i] (op) b[i] on device arrays of n doubles, through
+ * the FP64 arithmetic the KG_F64 sweeps run on the integer pipes (exact IEEE
+ * round-to-nearest-even addition, multiplication and division built from
+ * integer and FP32 operations: KG_ARITH_ADD/MUL/DIV) or through the FP64
+ * unit (KG_ARITH_NATIVE_*), so that the former can be checked bit for bit
+ * against IEEE arithmetic on any operands.  A verification entry point; no
+ * counterpart in the reference. */
+typedef enum {
+	KG_ARITH_ADD = 0,
+	KG_ARITH_MUL = 1,
+	KG_ARITH_DIV = 2,
+	KG_ARITH_NATIVE_ADD = 3,
+	KG_ARITH_NATIVE_MUL = 4,
+	KG_ARITH_NATIVE_DIV = 5
+} kg_arith_op;
+kg_status kg_exact_arith(int op, size_t n, const double* a, const double* b, double* out, kg_stream_t stream);
+
 /* Registers per thread of the kernel one sweep of (stencil, dt) launches. */
 kg_status kg_kernel_regcount(int stencil, kg_dtype dt, int* nregs);
 /* Kernel launches one sweep of (stencil, dt) makes (for launch counting). */

@@ -124,6 +124,61 @@ __device__ __forceinline__ double se_add(double a, double b)
 	return __longlong_as_double((long long)((X & 0x8000000000000000ull) | (((unsigned long long)(E - 1) << 52) + mant)));
 }
 
+static __device__ __noinline__ double se_native_div(double a, double b) { return __ddiv_rn(a, b); }
+
+// Small integers <-> FP32 without a conversion instruction: for |t| < 2^22
+// the float 1.5 * 2^23 + t has ulp 1, so its bit pattern is that of
+// 1.5 * 2^23 plus t (and a float x of magnitude below 2^22, added to
+// 1.5 * 2^23, is rounded to the nearest integer in the same way).
+__device__ __forceinline__ float se_i2f(int t) { return __fsub_rn(__int_as_float(0x4b400000 + t), 12582912.0f); }
+__device__ __forceinline__ int se_f2i_rn(float x) { return __float_as_int(__fadd_rn(x, 12582912.0f)) - 0x4b400000; }
+
+// Exact a / b, round to nearest even, by digit recurrence on the integer
+// significands: with N = ma or 2 ma (so that N / mb lies in [1, 2)), the 54-
+// bit floor Q of N 2^53 / mb is formed as three signed digits of 20, 20 and
+// 13 bits, Q = d1 2^33 + d2 2^13 + d3.  Each digit is estimated in FP32 from
+// the leading bits of the running remainder times an approximate reciprocal
+// of mb (rcp.approx of its leading 24 bits, relative error below 2^-22), and
+// the remainder is then updated exactly, R' = R 2^k - d mb, in 64-bit
+// integer arithmetic modulo 2^64 (the true remainders stay below 3.2 mb <
+// 2^55 in magnitude, so the wrapped values are exact).  The digit errors are
+// at most 2.2, 3.2 and 0.53 units, so one correction of the last digit makes
+// Q the exact floor and R its remainder in [0, mb).  Q's last bit is the
+// rounding bit; a tie (rounding bit set and R = 0) cannot occur for normal
+// operands but is rounded to even all the same.  Zeros, subnormals,
+// infinities, NaNs and quotients leaving the normal range go to the FP64
+// unit.
+__device__ __forceinline__ double se_div(double a, double b)
+{
+	const unsigned long long A = (unsigned long long)__double_as_longlong(a);
+	const unsigned long long B = (unsigned long long)__double_as_longlong(b);
+	const int ea = (int)(A >> 52) & 0x7ff, eb = (int)(B >> 52) & 0x7ff;
+	const unsigned long long ma = (A & 0xfffffffffffffull) | 0x10000000000000ull;
+	const unsigned long long mb = (B & 0xfffffffffffffull) | 0x10000000000000ull;
+	const int sh = ma < mb ? 1 : 0;
+	const unsigned long long N = ma << sh;                            // N / mb in [1, 2)
+	const int E = ea - eb - sh + 1023;
+	// rb ~ 2^52 / mb
+	float rb;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rb) : "f"(__int_as_float(0x3f800000 | (int)((mb >> 29) & 0x7fffff))));
+	const int d1 = se_f2i_rn(__fmul_rn(se_i2f((int)(N >> 32)), rb));                 // ~ N 2^20 / mb
+	const unsigned long long R1 = (N << 20) - (unsigned long long)(long long)d1 * mb;
+	const int d2 = se_f2i_rn(__fmul_rn(se_i2f((int)((long long)R1 >> 33)), 2.0f * rb));      // ~ R1 2^20 / mb
+	const unsigned long long R2 = (R1 << 20) - (unsigned long long)(long long)d2 * mb;
+	const int d3 = se_f2i_rn(__fmul_rn(se_i2f((int)((long long)R2 >> 33)), 0.015625f * rb)); // ~ R2 2^13 / mb
+	const unsigned long long R3 = (R2 << 13) - (unsigned long long)(long long)d3 * mb;
+	const unsigned long long neg = (unsigned long long)((long long)R3 < 0);
+	const unsigned long long Q = ((unsigned long long)(long long)d1 << 33) + ((unsigned long long)(long long)d2 << 13) +
+		(unsigned long long)(long long)d3 - neg;
+	const unsigned long long R = R3 + (neg ? mb : 0ull);
+	const unsigned long long mant0 = Q >> 1;
+	const unsigned long long mant = mant0 + ((Q & 1) & ((unsigned long long)(R != 0) | (mant0 & 1)));
+	const bool ok = (unsigned)(ea - 1) < 2046u && (unsigned)(eb - 1) < 2046u && E >= 1 && E <= 2045;
+	if (__builtin_expect(!ok, 0)) return se_native_div(a, b);
+	const unsigned long long sign = (A ^ B) & 0x8000000000000000ull;
+	return __longlong_as_double((long long)(sign | (((unsigned long long)(E - 1) << 52) + mant)));
+}
+
 __device__ __forceinline__ SE operator+(SE a, SE b) { return SE(se_add(a.v, b.v)); }
 __device__ __forceinline__ SE operator-(SE a, SE b)
 {

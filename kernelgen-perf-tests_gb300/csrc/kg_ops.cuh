@@ -43,6 +43,15 @@ template <class N> __device__ __forceinline__ N pm(N a, N b)
 	else return a * b;
 }
 
+// pdiv(a, b): a / b; in strict FP64 formed by the exact digit-recurrence
+// division on the integer and FP32 pipes (se_div; the same bits as the FP64
+// unit's quotient), which takes the division off the FP64 unit.
+template <class N> __device__ __forceinline__ N pdiv(N a, N b)
+{
+	if constexpr (std::is_same<N, SD>::value) return SD(se_div(a.v, b.v));
+	else return a / b;
+}
+
 // nsum(a, b, ...): a + b + ... added left to right, as written in the
 // reference.  For float-float, the terms' high parts go through a chain of
 // error-free TwoSums whose errors collect, with the low parts, in one FP32
@@ -139,7 +148,7 @@ template <class N> struct OpUxx1 {
 				at(d1, 0, 0, 0) + at(d1, 0, -1, 0) +
 				at(d1, 0, 0, -1) + at(d1, 0, -1, -1)));
 		}
-		o[0] = at(u0, 0, 0, 0) + pm(dth / d, nsum(
+		o[0] = at(u0, 0, 0, 0) + pm(pdiv(dth, d), nsum(
 			pm(c1, at(xx, 0, 0, 0) - at(xx, -1, 0, 0)),
 			pm(c2, at(xx, 1, 0, 0) - at(xx, -2, 0, 0)),
 			pm(c1, at(xy, 0, 0, 0) - at(xy, 0, -1, 0)),
@@ -396,7 +405,7 @@ template <class N> struct OpGameoflife {
 			at(u0, -1, -1, 0) + at(u0, 0, -1, 0) + at(u0, 1, -1, 0) +
 			at(u0, -1, 0, 0)                     + at(u0, 1, 0, 0) +
 			at(u0, -1, 1, 0) + at(u0, 0, 1, 0) + at(u0, 1, 1, 0);
-		o[0] = N(1.) / (N(1.) + pm(pm(at(u0, 0, 0, 0) + L - N(3.), L - N(3.)), C));
+		o[0] = pdiv(N(1.), N(1.) + pm(pm(at(u0, 0, 0, 0) + L - N(3.), L - N(3.)), C));
 	}
 };
 

@@ -39,10 +39,11 @@ EXPORTS = [
     "kg_batch_set_config", "kg_batch_get_config", "kg_batch_set_step", "kg_batch_final_roles",
     "kg_batch_destroy", "kg_poisson_solve", "kg_engine_status",
     "kg_vecadd", "kg_matvec", "kg_matmul", "kg_sincos", "kg_whispering", "kg_extra_regcount",
-    "kg_plan_kernels",
+    "kg_plan_kernels", "kg_exact_arith",
 ]
 EXTRA_TESTS = ["vecadd", "matvec", "matmul", "sincos", "whispering"]
 KG_ENGINE_AUTO, KG_ENGINE_DIRECT, KG_ENGINE_STAGED, KG_ENGINE_TMA = 0, 1, 2, 3
+KG_ARITH_ADD, KG_ARITH_MUL, KG_ARITH_DIV, KG_ARITH_NATIVE_ADD, KG_ARITH_NATIVE_MUL, KG_ARITH_NATIVE_DIV = range(6)
 ENGINES = {"auto": KG_ENGINE_AUTO, "direct": KG_ENGINE_DIRECT, "staged": KG_ENGINE_STAGED, "tma": KG_ENGINE_TMA}
 KG_SOLVE_SOR_F64, KG_SOLVE_IR_SOR_F32, KG_SOLVE_IR_JACOBI_F32 = 0, 1, 2
 
@@ -135,6 +136,7 @@ def _sig(lib):
         "kg_plan_final_roles": [P, ctypes.POINTER(KgProblem)],
         "kg_plan_destroy": [P],
         "kg_plan_kernels": [P],
+        "kg_exact_arith": [I, S, P, P, P, P],
         "kg_kernel_regcount": [I, I, ctypes.POINTER(I)],
         "kg_device_check": [],
         "kg_measure_peaks": [ctypes.POINTER(KgPeaks), P],
