@@ -683,7 +683,7 @@ def run_e2e(args, dtype, lanes=E2E_LANES):
     light = sorted((n for n in SUITE if n not in heavy), key=lambda nm: -(FP64_OPS_PER_PT[nm] + 2 * BYTES_PER_PT[nm]))
     if n_light == 0:
         heavy, light = heavy + light, []
-    errors = []
+    errors, once = [], []
 
     def lane(k, todo, lock):
         try:
@@ -694,7 +694,9 @@ def run_e2e(args, dtype, lanes=E2E_LANES):
                     name = todo.pop(0)
                 coef, arrs, _ = inputs[name]
                 p = kgb200.problem(name, dtype, shape_of(name), coef[:6], [a.ctypes.data for a in arrs])
-                kgb200.program_run(p, NT, result_mask(name), streams[k])
+                t = kgb200.program_run(p, NT, result_mask(name), streams[k])
+                if name in heavy:
+                    once.append(t.weights_once)
         except Exception as e:  # surfaced after the join
             errors.append(e)
 
@@ -716,16 +718,17 @@ def run_e2e(args, dtype, lanes=E2E_LANES):
         for _ in range(max(1, min(args.warmup, 2))):
             restore()
             step()
-        dt = 0.0
+        dt, each = 0.0, []
         for _ in range(args.steps):
             restore()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             step()
             torch.cuda.synchronize()
-            dt += time.perf_counter() - t0
+            each.append(time.perf_counter() - t0)
+            dt += each[-1]
     del inputs, pristine, pairs
-    return dt, h2d, d2h
+    return dt, h2d, d2h, each, all(once)
 
 
 # ---- the suite's other tests (vecadd, matvec, matmul, sincos, whispering) ----
@@ -998,10 +1001,11 @@ def main():
                     "produce the same bits)"},
     }
     if not args.no_e2e:
-        dt, h2d, d2h = run_e2e(args, dtype)
+        dt, h2d, d2h, each, once = run_e2e(args, dtype)
         dt = replica_max(dt, args.world)
         line["e2e"] = {"value": round(replica_value(args.world, pts_per_step, args.steps, dt), 4), "unit": "Gpts/s",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "step_ms": [round(t * 1e3, 1) for t in each], "tricubic_weights_once": once,
                        "path": "kg_program_run per stencil (stream-ordered alloc, H2D, 10 sweeps, D2H of the "
                                "checksum arrays, free) on pinned host arrays; the 11 programs on %d host threads with a "
                                "stream each (tricubic/tricubic2 on %d normal-priority, the rest on %d high-priority)"

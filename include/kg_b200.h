@@ -242,7 +242,8 @@ typedef struct {
 	double kernel_avg;      /* mean device time of one sweep (CUDA events)  */
 	double kernel_min;
 	int nregs;              /* registers per thread of the sweep kernel     */
-	int reserved;
+	int weights_once;       /* 1: tricubic's loop-invariant weight products
+	                           were evaluated once for the nt sweeps        */
 } kg_timings;
 
 /* Phases 2-6 of the reference main() (laplacian/laplacian.c:222-370) for one

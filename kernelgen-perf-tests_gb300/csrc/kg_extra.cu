@@ -24,6 +24,14 @@ template <class N> __device__ __forceinline__ N mul_on(N a, N b, bool integer)
 	else return a * b;
 }
 
+// Quotient a/b; for strict FP64 by the exact division on the integer and
+// FP32 pipes (se_div, the FP64 unit's bits).
+template <class N> __device__ __forceinline__ N div_on(N a, N b)
+{
+	if constexpr (std::is_same<N, SD>::value) return SD(se_div(a.v, b.v));
+	else return a / b;
+}
+
 // ---- vecadd/vecadd.c:38-84: w2 = w0 + w1 -----------------------------------
 
 template <class N, class S>
@@ -262,7 +270,7 @@ __global__ void __launch_bounds__(256) whispering_h_kernel(int nx, int ny, N mu,
 		const N ex = M(Cv::ld(ca + c - 1), Cv::ld(e + c - 1 + plane)) - M(Cv::ld(cb + c - 1), vh - Cv::ld(h0 + c - 1));
 		const N h = M(Cv::ld(da + c), vh) + M(Cv::ld(db + c), e0 - ey + ex - e1);
 		h1[c] = Cv::to(h);
-		u_em1[c] = Cv::to(Cv::ld(u_em0 + c) + M(N(0.5), M(h, h) / mu + M(epsilon, M(e0, e0) + M(e1, e1))));
+		u_em1[c] = Cv::to(Cv::ld(u_em0 + c) + M(N(0.5), div_on(M(h, h), mu) + M(epsilon, M(e0, e0) + M(e1, e1))));
 	}
 }
 

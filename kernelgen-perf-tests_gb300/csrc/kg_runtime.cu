@@ -197,6 +197,7 @@ kg_status kg_program_run(kg_problem* p, int nt, int copy_back_mask, kg_timings* 
 			t.kernel_min = mn;
 		}
 		kg_kernel_regcount(p->stencil, (kg_dtype)p->dtype, &t.nregs);
+		t.weights_once = pw ? 1 : 0;
 	}
 	for (int i = 0; i < made; i++) cudaEventDestroy(ev[i]);
 	delete[] ev;

@@ -89,7 +89,7 @@ class KgTimings(ctypes.Structure):
                 ("compute", ctypes.c_double), ("save", ctypes.c_double),
                 ("free_", ctypes.c_double), ("kernel_avg", ctypes.c_double),
                 ("kernel_min", ctypes.c_double), ("nregs", ctypes.c_int),
-                ("reserved", ctypes.c_int)]
+                ("weights_once", ctypes.c_int)]
 
 
 def build(jobs=8, drivers=True, quiet=True):
