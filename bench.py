@@ -345,15 +345,16 @@ def reference_final_means():
     return out
 
 
-# ---- precision sweep (wave13pt, uxx1; FP64 / FP32 / BF16) ------------------
+# ---- precision sweep (wave13pt, uxx1; FP64 / float-float / mixed / FP32 / BF16)
 
 PRECISION_SHAPE = (1024, 512, 512)
 
 
 def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt", "uxx1")):
     """The stencils advanced nsteps time steps from a Gaussian pulse (sigma 16
-    cells) + 1e-3 noise with stable coefficients, in FP64 (strict), FP32 and
-    BF16 storage with FP32 arithmetic, side by side.  Every `every` steps the
+    cells) + 1e-3 noise with stable coefficients, in FP64 (strict), FP64 with
+    float-float arithmetic, FP64 state with FP32 increments (uxx1), and FP32
+    and BF16 storage with FP32 arithmetic, side by side.  Every `every` steps the
     newest level of each narrow form is compared with FP64's (max and RMS of
     the difference relative to max and RMS of the FP64 field) and its FP64
     checksum taken.  Returns a dict per stencil."""
@@ -365,10 +366,13 @@ def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt"
     lib = kgb200.load()
     stream = torch.cuda.current_stream()
     sp = kgb200.stream_ptr(stream)
-    forms = [("f64", kgb200.KG_F64, torch.float64), ("f64ff", kgb200.KG_F64_FF, torch.float64),
-             ("f32", kgb200.KG_F32, torch.float32), ("bf16", kgb200.KG_BF16, torch.bfloat16)]
+    all_forms = [("f64", kgb200.KG_F64, torch.float64), ("f64ff", kgb200.KG_F64_FF, torch.float64),
+                 ("f64mix", kgb200.KG_F64_MIX, torch.float64),
+                 ("f32", kgb200.KG_F32, torch.float32), ("bf16", kgb200.KG_BF16, torch.bfloat16)]
     out = {}
     for name in names:
+        # the FP64-state / FP32-increment form is uxx1's (an incremental update)
+        forms = [f for f in all_forms if f[0] != "f64mix" or name == "uxx1"]
         inputs = make_inputs([name], variant=3, shape=shape)
         coef, arrs, _ = inputs[name]
         f64 = [torch.from_numpy(a).to("cuda") for a in arrs]
@@ -381,8 +385,8 @@ def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt"
         out_slot = 2 if name == "wave13pt" else 1
         stats = torch.zeros(4, dtype=torch.float64, device="cuda")
         sums = torch.zeros(1, dtype=torch.float64, device="cuda")
-        errs = {"f64ff": [], "f32": [], "bf16": []}
-        checks = {"f64": [], "f64ff": [], "f32": [], "bf16": []}
+        errs = {key: [] for key, _, _ in forms if key != "f64"}
+        checks = {key: [] for key, _, _ in forms}
         for block in range(nsteps // every):
             for key, dt, _ in forms:
                 st = state[key]
@@ -1013,7 +1017,8 @@ def main():
     if not args.no_forms:
         line["forms"] = {"fp64_float_float": ff_form, "precision_sweep": dict(
             workload="wave13pt and uxx1, 1024x512x512, 100 steps from a Gaussian pulse (sigma 16) + 1e-3 noise; "
-                     "FP64 strict vs FP32 and BF16 storage (FP32 arithmetic); errors relative to FP64 every 10 steps",
+                     "FP64 strict vs float-float (f64ff), FP64 state with FP32 increments (f64mix, uxx1), FP32 and "
+                     "BF16 storage (FP32 arithmetic); errors relative to FP64 every 10 steps",
             **run_precision())}
         line["forms"]["batched"] = run_batched(tune_cache=os.environ.get("KG_TUNE_CACHE"))
         line["forms"]["iterative_refinement"] = dict(

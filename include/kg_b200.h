@@ -51,9 +51,13 @@ typedef enum {
 	KG_BF16 = 3,     /* BF16 storage, FP32 arithmetic                         */
 	KG_F16 = 4,      /* FP16 storage, FP32 arithmetic                         */
 	KG_U8 = 5,       /* 0/1 byte cells: gameoflife only (B3/S23)              */
-	KG_F64_FF = 6    /* FP64 storage; arithmetic on float-float pairs (hi+lo
+	KG_F64_FF = 6,   /* FP64 storage; arithmetic on float-float pairs (hi+lo
 	                    FP32 with error-free transformations) on the FP32 pipes:
 	                    ~1e-14 of FP64 normwise, values within FP32's range    */
+	KG_F64_MIX = 7   /* FP64 storage; each step's increment in FP32 arithmetic,
+	                    added to the FP64 state in FP64 (uxx1 only: the state
+	                    keeps FP64 precision, a step errs by FP32's relative
+	                    error of its increment)                                */
 } kg_dtype;
 
 /* Stencil ids (the suite's test directories). */

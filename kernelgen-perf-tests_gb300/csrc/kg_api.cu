@@ -41,7 +41,7 @@ kg_status fail_cuda(cudaError_t e, const char* what)
 size_t dtype_size(int dt)
 {
 	switch (dt) {
-	case KG_F64: case KG_F64_FMA: case KG_F64_FF: return 8;
+	case KG_F64: case KG_F64_FMA: case KG_F64_FF: case KG_F64_MIX: return 8;
 	case KG_F32: return 4;
 	case KG_BF16: case KG_F16: return 2;
 	case KG_U8: return 1;
@@ -66,7 +66,7 @@ static int engines_built(int dt)
 	case KG_F64: case KG_F64_FMA: return d | t;
 	case KG_F64_FF: return st | t;
 	case KG_F32: case KG_BF16: case KG_F16: return d | t | (KG_FF_STAGED ? st : 0);
-	case KG_U8: return d;
+	case KG_U8: case KG_F64_MIX: return d;
 	default: return 0;
 	}
 }
@@ -83,7 +83,9 @@ static kg_status validate(const kg_problem* p)
 	if (!p) return fail(KG_EINVAL, "null problem");
 	if (p->stencil < 0 || p->stencil >= KG_NSTENCILS) return fail(KG_EINVAL, "unknown stencil %d", p->stencil);
 	const Meta& m = k_meta[p->stencil];
-	if (p->dtype < KG_F64 || p->dtype > KG_F64_FF) return fail(KG_EINVAL, "%s: unknown dtype %d", m.name, p->dtype);
+	if (p->dtype < KG_F64 || p->dtype > KG_F64_MIX) return fail(KG_EINVAL, "%s: unknown dtype %d", m.name, p->dtype);
+	if (p->dtype == KG_F64_MIX && p->stencil != KG_UXX1)
+		return fail(KG_ENOTSUP, "%s: the FP64-state / FP32-increment form is provided for uxx1 only", m.name);
 	if (p->dtype == KG_U8 && p->stencil != KG_GAMEOFLIFE)
 		return fail(KG_ENOTSUP, "%s: byte cells are provided for gameoflife only", m.name);
 	if (p->nx < 0 || p->ny < 0 || p->ns < 0) return fail(KG_EINVAL, "%s: negative size", m.name);
@@ -124,6 +126,7 @@ static cudaError_t dispatch(const kg_problem& p, cudaStream_t st)
 	case KG_BF16: return sweep_bf16(p, st);
 	case KG_F16: return sweep_f16(p, st);
 	case KG_U8: return sweep_u8(p, st);
+	case KG_F64_MIX: return sweep_uxx1_mix(p, st);
 	default: return cudaErrorInvalidValue;
 	}
 }
@@ -286,6 +289,10 @@ kg_status kg_kernel_regcount(int stencil, kg_dtype dt, int* nregs)
 	case KG_U8:
 		if (stencil != KG_GAMEOFLIFE) return fail(KG_ENOTSUP, "byte cells: gameoflife only");
 		e = regs_u8(p, nregs);
+		break;
+	case KG_F64_MIX:
+		if (stencil != KG_UXX1) return fail(KG_ENOTSUP, "the FP64-state / FP32-increment form: uxx1 only");
+		e = regs_uxx1_mix(nregs);
 		break;
 	default: return fail(KG_EINVAL, "kg_kernel_regcount: unknown dtype");
 	}

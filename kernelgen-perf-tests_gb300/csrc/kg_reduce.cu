@@ -243,7 +243,7 @@ extern "C" kg_status kg_checksum_noalloc(kg_dtype dt, size_t n, int narr, const 
 	if (s != KG_OK) return s;
 	cudaError_t e;
 	switch (dt) {
-	case KG_F64: case KG_F64_FMA: case KG_F64_FF: e = checksum_static_t<double>(n, A, partial, out_dev, st); break;
+	case KG_F64: case KG_F64_FMA: case KG_F64_FF: case KG_F64_MIX: e = checksum_static_t<double>(n, A, partial, out_dev, st); break;
 	case KG_F32: e = checksum_static_t<float>(n, A, partial, out_dev, st); break;
 	case KG_BF16: e = checksum_static_t<__nv_bfloat16>(n, A, partial, out_dev, st); break;
 	case KG_F16: e = checksum_static_t<__half>(n, A, partial, out_dev, st); break;
@@ -268,7 +268,7 @@ extern "C" kg_status kg_checksum(kg_dtype dt, size_t n, int narr, const void* co
 	cudaStream_t st = (cudaStream_t)stream;
 	cudaError_t e;
 	switch (dt) {
-	case KG_F64: case KG_F64_FMA: case KG_F64_FF: e = checksum_t<double>(n, A, out_dev, st); break;
+	case KG_F64: case KG_F64_FMA: case KG_F64_FF: case KG_F64_MIX: e = checksum_t<double>(n, A, out_dev, st); break;
 	case KG_F32: e = checksum_t<float>(n, A, out_dev, st); break;
 	case KG_BF16: e = checksum_t<__nv_bfloat16>(n, A, out_dev, st); break;
 	case KG_F16: e = checksum_t<__half>(n, A, out_dev, st); break;
@@ -287,7 +287,7 @@ extern "C" kg_status kg_error_stats(kg_dtype dt, size_t n, const void* x, const 
 	if (n == 0) return fail_cuda(cudaMemsetAsync(out_dev, 0, 4 * sizeof(double), st), "kg_error_stats");
 	cudaError_t e;
 	switch (dt) {
-	case KG_F64: case KG_F64_FMA: case KG_F64_FF: e = errstats_t<double>(n, x, ref, out_dev, st); break;
+	case KG_F64: case KG_F64_FMA: case KG_F64_FF: case KG_F64_MIX: e = errstats_t<double>(n, x, ref, out_dev, st); break;
 	case KG_F32: e = errstats_t<float>(n, x, ref, out_dev, st); break;
 	case KG_BF16: e = errstats_t<__nv_bfloat16>(n, x, ref, out_dev, st); break;
 	case KG_F16: e = errstats_t<__half>(n, x, ref, out_dev, st); break;
@@ -303,11 +303,11 @@ extern "C" kg_status kg_convert(kg_dtype dst_t, void* dst, kg_dtype src_t, const
 	clear_error();
 	if (n && (!dst || !src)) return fail(KG_EINVAL, "kg_convert: null pointer");
 	cudaStream_t st = (cudaStream_t)stream;
-	auto is64 = [](kg_dtype t) { return t == KG_F64 || t == KG_F64_FMA || t == KG_F64_FF; };
+	auto is64 = [](kg_dtype t) { return t == KG_F64 || t == KG_F64_FMA || t == KG_F64_FF || t == KG_F64_MIX; };
 	cudaError_t e = cudaErrorInvalidValue;
 	if (is64(src_t)) {
 		switch (dst_t) {
-		case KG_F64: case KG_F64_FMA: case KG_F64_FF: e = convert_t<double, double>(dst, src, n, st); break;
+		case KG_F64: case KG_F64_FMA: case KG_F64_FF: case KG_F64_MIX: e = convert_t<double, double>(dst, src, n, st); break;
 		case KG_F32: e = convert_t<float, double>(dst, src, n, st); break;
 		case KG_BF16: e = convert_t<__nv_bfloat16, double>(dst, src, n, st); break;
 		case KG_F16: e = convert_t<__half, double>(dst, src, n, st); break;

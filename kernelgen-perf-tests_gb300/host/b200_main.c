@@ -8,7 +8,8 @@
  *
  * Knobs (environment, set by the target makefile from make variables):
  *   B200_PREC  fp64 (default; bitwise = IEEE reference) | fp64fma | fp64ff
- *              (FP64 storage, float-float arithmetic) | fp32 | bf16 | fp16 |
+ *              (FP64 storage, float-float arithmetic) | fp64mix (uxx1: FP64
+ *              state, FP32 increments) | fp32 | bf16 | fp16 |
  *              u8 (gameoflife on 0/1 byte cells)
  *   B200_INIT  reference (default) | bernoulli | unit | pulse
  *   B200_MODE  plain (default: one launch per sweep, timed) | graph (the
@@ -69,6 +70,7 @@ static kg_dtype parse_prec(const char* s)
 	if (!strcmp(s, "fp16")) return KG_F16;
 	if (!strcmp(s, "u8")) return KG_U8;
 	if (!strcmp(s, "fp64ff")) return KG_F64_FF;
+	if (!strcmp(s, "fp64mix")) return KG_F64_MIX;
 	fprintf(stderr, "Unknown B200_PREC=%s\n", s);
 	exit(1);
 }
@@ -130,7 +132,7 @@ int main(int argc, char* argv[])
 	const int narr = kg_stencil_narrays(test);
 	const size_t n = (size_t)nx * ny * ns;
 	const size_t szb64 = n * sizeof(double);
-	const size_t es = (dt == KG_F64 || dt == KG_F64_FMA || dt == KG_F64_FF) ? 8 : (dt == KG_F32) ? 4 : (dt == KG_U8) ? 1 : 2;
+	const size_t es = (dt == KG_F64 || dt == KG_F64_FMA || dt == KG_F64_FF || dt == KG_F64_MIX) ? 8 : (dt == KG_F32) ? 4 : (dt == KG_U8) ? 1 : 2;
 	const size_t szb = n * es;
 
 	double coef[6];

@@ -20,10 +20,10 @@ STENCILS = ["laplacian", "divergence", "gradient", "uxx1", "wave13pt", "tricubic
 STENCIL_ID = {s: i for i, s in enumerate(STENCILS)}
 IS2D = {"jacobi", "gaussblur", "gameoflife"}
 
-KG_F64, KG_F64_FMA, KG_F32, KG_BF16, KG_F16, KG_U8, KG_F64_FF = range(7)
+KG_F64, KG_F64_FMA, KG_F32, KG_BF16, KG_F16, KG_U8, KG_F64_FF, KG_F64_MIX = range(8)
 DTYPES = {"f64": KG_F64, "f64fma": KG_F64_FMA, "f32": KG_F32, "bf16": KG_BF16,
-          "f16": KG_F16, "u8": KG_U8, "f64ff": KG_F64_FF}
-DTYPE_SIZE = {KG_F64: 8, KG_F64_FMA: 8, KG_F32: 4, KG_BF16: 2, KG_F16: 2, KG_U8: 1, KG_F64_FF: 8}
+          "f16": KG_F16, "u8": KG_U8, "f64ff": KG_F64_FF, "f64mix": KG_F64_MIX}
+DTYPE_SIZE = {KG_F64: 8, KG_F64_FMA: 8, KG_F32: 4, KG_BF16: 2, KG_F16: 2, KG_U8: 1, KG_F64_FF: 8, KG_F64_MIX: 8}
 STATUS = ["KG_OK", "KG_EINVAL", "KG_ECUDA", "KG_ENOMEM", "KG_ETIMEOUT", "KG_ENOTSUP", "KG_ENODEV"]
 
 # Every extern "C" symbol the header declares (checked by the CPU tests).

@@ -22,8 +22,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 # The leapfrog wave update carries every rounding forward undamped, so its
 # error grows fastest (measured at 1024x512x512: FP32 1.2e-5 after 20 steps,
 # 1.1e-4 after 100; BF16 0.5 after 40); uxx1 accumulates linearly.
+# uxx1's KG_F64_MIX form (FP64 state, FP32 increments) keeps the state's
+# precision: its error is FP32's relative error of the small increments.
 TOL = {"wave13pt": {kgb200.KG_F32: 1e-4, kgb200.KG_BF16: 0.5},
-       "uxx1": {kgb200.KG_F32: 1e-5, kgb200.KG_BF16: 2e-2}}
+       "uxx1": {kgb200.KG_F32: 1e-5, kgb200.KG_BF16: 2e-2, kgb200.KG_F64_MIX: 1e-7}}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -51,8 +53,10 @@ def test_precision_sweep_small(name):
     case = ol.Case.from_arrays(name, shape, coef, arrs)
     out_slot = 2 if name == "wave13pt" else 1
     runs = {}
-    for dt, tdt in ((kgb200.KG_F64, torch.float64), (kgb200.KG_F32, torch.float32),
-                    (kgb200.KG_BF16, torch.bfloat16)):
+    forms = [(kgb200.KG_F64, torch.float64), (kgb200.KG_F32, torch.float32), (kgb200.KG_BF16, torch.bfloat16)]
+    if name == "uxx1":
+        forms.append((kgb200.KG_F64_MIX, torch.float64))
+    for dt, tdt in forms:
         bufs = [torch.from_numpy(a).cuda().to(tdt) for a in arrs]
         runs[dt] = {"bufs": bufs, "ptrs": [b.data_ptr() for b in bufs]}
     stats = torch.zeros(4, dtype=torch.float64, device="cuda")
@@ -69,11 +73,41 @@ def test_precision_sweep_small(name):
         g = by[newest[kgb200.KG_F64]].cpu().numpy()
         want = case.arrays()[1 if name == "wave13pt" else 0]
         assert np.array_equal(g.view(np.uint64), want.view(np.uint64)), "FP64 differs from the oracle"
-        for dt in (kgb200.KG_F32, kgb200.KG_BF16):
+        for dt in [d for d, _ in forms[1:]]:
             kgb200.error_stats(dt, n, newest[dt], newest[kgb200.KG_F64], stats.data_ptr())
             mx, s2, mref, sref2 = stats.tolist()
             assert np.isfinite(mx) and mx / mref <= TOL[name][dt], (name, dt, block, mx / mref)
         assert np.all(np.isfinite(g))
+
+
+@pytest.mark.parametrize("shape", [(3, 3, 3), (4, 4, 4), (5, 7, 6), (64, 32, 32), (129, 35, 20)])
+def test_uxx1_mixed_form(shape):
+    """KG_F64_MIX uxx1 on the reference's random inputs: within 1e-6 of the
+    oracle normwise after 4 sweeps (rims untouched, bit for bit)."""
+    from test_parity_gpu import gpu_run, normwise
+    case = ol.Case("uxx1", shape)
+    nt = 4
+    got = gpu_run("uxx1", kgb200.KG_F64_MIX, case.shape, case.coef, [a.copy() for a in case.arrays()], nt)
+    case.run(nt)
+    for g, w in zip(got, case.arrays()):
+        assert normwise(g, w) <= 1e-6, normwise(g, w)
+        nx, ny, ns = shape
+        gg, ww = g.reshape(ns, ny, nx), w.reshape(ns, ny, nx)
+        for sl in ((slice(None), slice(None), slice(0, 2)), (slice(None), slice(None), slice(nx - 1, nx)),
+                   (slice(None), slice(0, 2), slice(None)), (slice(0, 2), slice(None), slice(None)),
+                   (slice(ns - 1, ns), slice(None), slice(None))):
+            assert np.array_equal(gg[sl].view(np.uint64), ww[sl].view(np.uint64))
+
+
+def test_mixed_form_is_uxx1_only():
+    lib = kgb200.load()
+    a = torch.zeros(6 * 512, dtype=torch.float64, device="cuda")
+    ptrs = [a.data_ptr() + 8 * 512 * q for q in range(6)]
+    for name in kgb200.STENCILS:
+        p = kgb200.problem(name, kgb200.KG_F64_MIX, (8, 8) if name in kgb200.IS2D else (8, 8, 8), [0.5] * 6, ptrs)
+        want = 0 if name == "uxx1" else 5
+        assert lib.kg_sweep(ctypes.byref(p), None) == want, name
+    torch.cuda.synchronize()
 
 
 FF_NAMES = [n for n in kgb200.STENCILS if n != "gameoflife"]
