@@ -33,19 +33,33 @@ __device__ __forceinline__ SD operator/(SD a, SD b) { return SD(__ddiv_rn(a.v, b
 // Additions, subtractions and multiplications are exact IEEE round-to-
 // nearest-even operations built from 32-bit integer arithmetic (53-bit
 // mantissas in two words, 106-bit products from four 32x32 multiplies,
-// guard/round/sticky rounding), so their bits equal the FP64 unit's.  Zeros,
-// subnormals, infinities, NaNs and results leaving the normal range take a
-// rarely used branch to the FP64 unit; division always does.  GB300 issues
+// guard/round/sticky rounding), so their bits equal the FP64 unit's; se_div
+// (below) divides.  Zeros, subnormals, infinities, NaNs and results leaving
+// the normal range take a rarely used branch to the FP64 unit.  GB300 issues
 // FP64 arithmetic at 1/72 of its FP32 rate while the integer pipes sit idle
 // in these sweeps: measured, a thread that interleaves independent native
-// and integer multiplies reaches 1.9x the FP64 unit's multiply rate, bit for
-// bit the same (strict tricubic uses this).  Whole warps computing in SE
-// beside warps in SD were slower: the stencils' sums are dependent chains.
+// and integer multiplies reaches 1.9x the FP64 unit's multiply rate, and
+// additions 1.3x, bit for bit the same.  The strict sweeps form their
+// products (pm), quotients (pdiv) and a share of every sum's additions (nsum)
+// this way, within each thread; whole warps computing in SE beside warps in
+// SD were slower.
 struct SE {
 	double v;
 	__host__ __device__ constexpr SE() : v(0) {}
 	__host__ __device__ constexpr explicit SE(double x) : v(x) {}
 };
+
+// a < b for 64-bit unsigned integers from 32-bit comparisons of their words:
+// a 64-bit integer comparison issues to the FP64 pipe on GB300, which the
+// integer-pipe arithmetic below exists to leave to the native operations.
+__device__ __forceinline__ bool se_lt_u64(unsigned long long a, unsigned long long b)
+{
+	unsigned lt_hi, eq_hi, lt_lo;
+	asm("set.lt.u32.u32 %0, %1, %2;" : "=r"(lt_hi) : "r"((unsigned)(a >> 32)), "r"((unsigned)(b >> 32)));
+	asm("set.eq.u32.u32 %0, %1, %2;" : "=r"(eq_hi) : "r"((unsigned)(a >> 32)), "r"((unsigned)(b >> 32)));
+	asm("set.lt.u32.u32 %0, %1, %2;" : "=r"(lt_lo) : "r"((unsigned)a), "r"((unsigned)b));
+	return (lt_hi | (eq_hi & lt_lo)) != 0;
+}
 
 static __device__ __noinline__ double se_native_mul(double a, double b) { return __dmul_rn(a, b); }
 static __device__ __noinline__ double se_native_add(double a, double b) { return __dadd_rn(a, b); }
@@ -82,17 +96,16 @@ __device__ __forceinline__ double se_mul(double a, double b)
 // Exact a + b.  Branch-free apart from the rare fallback, so warps whose
 // lanes add operands of mixed signs do not diverge: both the same-sign sum
 // and the opposite-sign difference are formed and one is selected.
-// Measured on GB300: 0.26e12 additions/s alone against the FP64 unit's 0.50e12,
-// and no gain when mixed with it (a quarter or half of independent additions
-// on the integer pipes: 0.497 and 0.483e12/s); moving a stencil's neighbour
-// sums here made every strict sweep slower (laplacian 0.51 -> 0.64 ms,
-// lapgsrb 1.73 -> 2.41, gaussblur 1.98 -> 2.42 at 512x256x256), so only
-// products (se_mul) are moved, in tricubic.
+// Measured on GB300 (independent additions): 0.26e12/s alone against the
+// FP64 unit's 0.50e12; a quarter or three eighths of them here and the rest
+// on the FP64 unit, 0.65 and 0.66e12/s together (with the magnitude
+// comparison as one 64-bit integer comparison, which issues to the FP64
+// pipe, mixing gained nothing: 0.49e12/s).
 __device__ __forceinline__ double se_add(double a, double b)
 {
 	const unsigned long long A = (unsigned long long)__double_as_longlong(a);
 	const unsigned long long B = (unsigned long long)__double_as_longlong(b);
-	const bool sw = (A & 0x7fffffffffffffffull) < (B & 0x7fffffffffffffffull);
+	const bool sw = se_lt_u64(A & 0x7fffffffffffffffull, B & 0x7fffffffffffffffull);   // |a| < |b|
 	const unsigned long long X = sw ? B : A, Y = sw ? A : B;         // |X| >= |Y|
 	const int ex = (int)(X >> 52) & 0x7ff, ey = (int)(Y >> 52) & 0x7ff;
 	const bool ok_in = (unsigned)(ex - 1) < 2046u && (unsigned)(ey - 1) < 2046u;
@@ -155,7 +168,7 @@ __device__ __forceinline__ double se_div(double a, double b)
 	const int ea = (int)(A >> 52) & 0x7ff, eb = (int)(B >> 52) & 0x7ff;
 	const unsigned long long ma = (A & 0xfffffffffffffull) | 0x10000000000000ull;
 	const unsigned long long mb = (B & 0xfffffffffffffull) | 0x10000000000000ull;
-	const int sh = ma < mb ? 1 : 0;
+	const int sh = se_lt_u64(ma, mb) ? 1 : 0;
 	const unsigned long long N = ma << sh;                            // N / mb in [1, 2)
 	const int E = ea - eb - sh + 1023;
 	// rb ~ 2^52 / mb

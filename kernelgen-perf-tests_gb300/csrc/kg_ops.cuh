@@ -58,9 +58,27 @@ template <class N> __device__ __forceinline__ N pdiv(N a, N b)
 // accumulator, renormalised once at the end (8 instead of 10 FP32 operations
 // per term; the same ~2^-48 relative bound).  Other types: plain binary adds,
 // the same operations as the expression (bit for bit).
-template <class N, class... T> __device__ __forceinline__ N nsum(N a, T... rest)
+// Strict FP64: the first K additions of the chain on the integer pipes
+// (se_add), the rest on the FP64 unit; the same bits either way.  Each op
+// picks K per sum (measured at 512x256x256 / 512x65536, ms per sweep, K = 0 ->
+// 1 -> 2 for every sum of the op: laplacian 0.383 / 0.322 / 0.398, uxx1
+// 0.958 / 0.931 / 1.166, wave13pt 0.809 / 0.689 / 0.723, jacobi 0.517 / 0.456
+// / 0.684, lapgsrb 1.490 / 1.302 / 1.150, gaussblur 1.541 / 1.230 / 1.644,
+// gameoflife 0.704 / 0.647 / 0.594): a sum's chain shares the FP64 unit with
+// the integer pipes, which also form the products.
+template <int I, int K> __device__ __forceinline__ double nsum_sd(double acc) { return acc; }
+template <int I, int K, class... T> __device__ __forceinline__ double nsum_sd(double acc, SD x, T... rest)
 {
-	if constexpr (std::is_same<N, FF2>::value) {
+	if constexpr (I < K) acc = se_add(acc, x.v);
+	else acc = __dadd_rn(acc, x.v);
+	return nsum_sd<I + 1, K>(acc, rest...);
+}
+
+template <int K = 0, class N, class... T> __device__ __forceinline__ N nsum(N a, T... rest)
+{
+	if constexpr (std::is_same<N, SD>::value) {
+		return SD(nsum_sd<0, K>(a.v, rest...));
+	} else if constexpr (std::is_same<N, FF2>::value) {
 		float s = a.hi, e = a.lo;
 		auto add = [&](FF2 x) {
 			const float t = __fadd_rn(s, x.hi);
@@ -85,7 +103,7 @@ template <class N> struct OpLaplacian {
 	N alpha, beta;
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w0 = 0;
-		o[0] = pm(alpha, at(w0, 0, 0, 0)) + pm(beta, nsum(
+		o[0] = pm(alpha, at(w0, 0, 0, 0)) + pm(beta, nsum<1>(
 			at(w0, 1, 0, 0), at(w0, -1, 0, 0),
 			at(w0, 0, 1, 0), at(w0, 0, -1, 0),
 			at(w0, 0, 0, 1), at(w0, 0, 0, -1)));
@@ -144,11 +162,11 @@ template <class N> struct OpUxx1 {
 				at.raw(d1, 0, 0, 0) + at.raw(d1, 0, -1, 0) +
 				at.raw(d1, 0, 0, -1) + at.raw(d1, 0, -1, -1)));
 		} else {
-			d = pm(N(0.25), (
-				at(d1, 0, 0, 0) + at(d1, 0, -1, 0) +
-				at(d1, 0, 0, -1) + at(d1, 0, -1, -1)));
+			d = pm(N(0.25), nsum<1>(
+				at(d1, 0, 0, 0), at(d1, 0, -1, 0),
+				at(d1, 0, 0, -1), at(d1, 0, -1, -1)));
 		}
-		o[0] = at(u0, 0, 0, 0) + pm(pdiv(dth, d), nsum(
+		o[0] = at(u0, 0, 0, 0) + pm(pdiv(dth, d), nsum<1>(
 			pm(c1, at(xx, 0, 0, 0) - at(xx, -1, 0, 0)),
 			pm(c2, at(xx, 1, 0, 0) - at(xx, -2, 0, 0)),
 			pm(c1, at(xy, 0, 0, 0) - at(xy, 0, -1, 0)),
@@ -167,11 +185,11 @@ template <class N> struct OpWave13pt {
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w0 = 0, w1 = 1;
 		o[0] = pm(m0, at(w1, 0, 0, 0)) - at(w0, 0, 0, 0) +
-			pm(m1, nsum(
+			pm(m1, nsum<1>(
 				at(w1, 1, 0, 0), at(w1, -1, 0, 0),
 				at(w1, 0, 1, 0), at(w1, 0, -1, 0),
 				at(w1, 0, 0, 1), at(w1, 0, 0, -1))) +
-			pm(m2, nsum(
+			pm(m2, nsum<1>(
 				at(w1, 2, 0, 0), at(w1, -2, 0, 0),
 				at(w1, 0, 2, 0), at(w1, 0, -2, 0),
 				at(w1, 0, 0, 2), at(w1, 0, 0, -2)));
@@ -344,8 +362,8 @@ template <class N> struct OpJacobi {
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w0 = 0;
 		o[0] = pm(c0, at(w0, 0, 0, 0)) +
-			pm(c1, nsum(at(w0, -1, 0, 0), at(w0, 0, -1, 0), at(w0, 1, 0, 0), at(w0, 0, 1, 0))) +
-			pm(c2, nsum(at(w0, -1, -1, 0), at(w0, -1, 1, 0), at(w0, 1, -1, 0), at(w0, 1, 1, 0)));
+			pm(c1, nsum<1>(at(w0, -1, 0, 0), at(w0, 0, -1, 0), at(w0, 1, 0, 0), at(w0, 0, 1, 0))) +
+			pm(c2, nsum<1>(at(w0, -1, -1, 0), at(w0, -1, 1, 0), at(w0, 1, -1, 0), at(w0, 1, 1, 0)));
 	}
 };
 
@@ -358,15 +376,15 @@ template <class N> struct OpLapgsrb {
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int w = 0;
 		o[0] = pm(c0, at(w, 0, 0, 0)) +
-			pm(c1, nsum(
+			pm(c1, nsum<2>(
 				at(w, 1, 0, 0), at(w, -1, 0, 0),
 				at(w, 0, 1, 0), at(w, 0, -1, 0),
 				at(w, 0, 0, 1), at(w, 0, 0, -1))) +
-			pm(c2, nsum(
+			pm(c2, nsum<2>(
 				at(w, 1, 1, 0), at(w, 1, 0, 1), at(w, 1, 0, -1), at(w, 1, -1, 0),
 				at(w, 0, 1, 1), at(w, 0, 1, -1), at(w, 0, -1, 1), at(w, 0, -1, -1),
 				at(w, -1, 1, 0), at(w, -1, 0, 1), at(w, -1, 0, -1), at(w, -1, -1, 0))) +
-			pm(c3, nsum(
+			pm(c3, nsum<2>(
 				at(w, 2, 0, 0), at(w, -2, 0, 0),
 				at(w, 0, 2, 0), at(w, 0, -2, 0),
 				at(w, 0, 0, 2), at(w, 0, 0, -2)));
@@ -384,12 +402,12 @@ template <class N> struct OpGaussblur {
 		const int w = 0;
 		o[0] = pm(f, (
 			pm(s0, at(w, 0, 0, 0)) +
-			pm(s1, nsum(at(w, -1, 0, 0), at(w, 1, 0, 0), at(w, 0, -1, 0), at(w, 0, 1, 0))) +
-			pm(s2, nsum(at(w, -1, -1, 0), at(w, 1, -1, 0), at(w, -1, 1, 0), at(w, 1, 1, 0))) +
-			pm(s4, nsum(at(w, -2, 0, 0), at(w, 2, 0, 0), at(w, 0, -2, 0), at(w, 0, 2, 0))) +
-			pm(s5, nsum(at(w, -2, -1, 0), at(w, -1, -2, 0), at(w, 1, -2, 0), at(w, 2, -1, 0),
+			pm(s1, nsum<1>(at(w, -1, 0, 0), at(w, 1, 0, 0), at(w, 0, -1, 0), at(w, 0, 1, 0))) +
+			pm(s2, nsum<1>(at(w, -1, -1, 0), at(w, 1, -1, 0), at(w, -1, 1, 0), at(w, 1, 1, 0))) +
+			pm(s4, nsum<1>(at(w, -2, 0, 0), at(w, 2, 0, 0), at(w, 0, -2, 0), at(w, 0, 2, 0))) +
+			pm(s5, nsum<1>(at(w, -2, -1, 0), at(w, -1, -2, 0), at(w, 1, -2, 0), at(w, 2, -1, 0),
 			      at(w, -2, 1, 0), at(w, -1, 2, 0), at(w, 1, 2, 0), at(w, 2, 1, 0))) +
-			pm(s8, nsum(at(w, -2, -2, 0), at(w, 2, -2, 0), at(w, -2, 2, 0), at(w, 2, 2, 0)))));
+			pm(s8, nsum<1>(at(w, -2, -2, 0), at(w, 2, -2, 0), at(w, -2, 2, 0), at(w, 2, 2, 0)))));
 	}
 };
 
@@ -401,10 +419,10 @@ template <class N> struct OpGameoflife {
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int u0 = 0;
 		const N C(100000000000000000000.);
-		N L =
-			at(u0, -1, -1, 0) + at(u0, 0, -1, 0) + at(u0, 1, -1, 0) +
-			at(u0, -1, 0, 0)                     + at(u0, 1, 0, 0) +
-			at(u0, -1, 1, 0) + at(u0, 0, 1, 0) + at(u0, 1, 1, 0);
+		N L = nsum<2>(
+			at(u0, -1, -1, 0), at(u0, 0, -1, 0), at(u0, 1, -1, 0),
+			at(u0, -1, 0, 0),                    at(u0, 1, 0, 0),
+			at(u0, -1, 1, 0), at(u0, 0, 1, 0), at(u0, 1, 1, 0));
 		o[0] = pdiv(N(1.), N(1.) + pm(pm(at(u0, 0, 0, 0) + L - N(3.), L - N(3.)), C));
 	}
 };

@@ -24,9 +24,23 @@ namespace kg {
 
 // Products pw * u0 formed by the exact integer multiply: x-neighbours ii <
 // kTriPwEmu of every (jj, kk) row.  Measured on GB300 (512x256x256, weights
-// once + 10 sweeps, ms): 0 of 4: 85.6; 1: 75.7; 2: 65.9; 3: 56.7; 4: 61.5
-// (10 sweeps computing the weights inline: 118.7).
-constexpr int kTriPwEmu = 3;
+// once + 10 sweeps, ms, all additions on the FP64 unit): 0 of 4: 85.6; 1:
+// 75.7; 2: 65.9; 3: 56.7; 4: 61.5 (10 sweeps computing the weights inline:
+// 118.7).
+#ifndef KG_PW_EMU
+#define KG_PW_EMU 3
+#endif
+constexpr int kTriPwEmu = KG_PW_EMU;
+
+#ifndef KG_PW_ADD_INT
+#define KG_PW_ADD_INT 1
+#endif
+// Additions of the in-order sum on the integer pipes (se_add): the first
+// kTriPwAddInt of every run of 16 terms (one kk).  Measured (ms per sweep,
+// tricubic / tricubic2, products on the integer pipes 3 of 4): 0 additions
+// 5.686 / 5.824, 1: 5.652 / 5.698, 2: 5.787 / 5.780; with 2 of 4 products
+// and 2 or 4 additions 6.104 / 6.272 and 5.822 / 5.903.
+constexpr int kTriPwAddInt = KG_PW_ADD_INT;
 
 constexpr int kPwBX = 32, kPwBY = 8, kPwKC = 8;
 
@@ -107,6 +121,8 @@ __global__ void __launch_bounds__(kPwBX * kPwBY, 3) tricubic_pw_sweep_kernel(int
 					else
 						t = N(wv) * N(u);
 					if (m == 0) s = FROM_ZERO ? N(0.0) + t : t;
+					else if constexpr (std::is_same<N, SD>::value)
+						s = SD((m & 15) != 0 && (m & 15) <= kTriPwAddInt ? se_add(s.v, t.v) : __dadd_rn(s.v, t.v));
 					else s = s + t;
 				}
 		u1[c] = s.v;
