@@ -36,7 +36,7 @@ struct Halo {
 // / 0.323, gradient 0.384 / 0.263 / 0.245, uxx1 1.910 / 1.722 / 1.406,
 // wave13pt 0.992 / 0.870 / 0.808, jacobi 0.704 / 0.580 / 0.517, lapgsrb 1.729
 // / 1.609 / 1.488, gaussblur 1.974 / 1.723 / 1.540, gameoflife 1.127 / 1.065
-// / 1.000.  Additions do not move (se_add in kg_num.cuh).
+// / 1.000.  A share of each sum's additions moves too (nsum<K>, below).
 template <class N> __device__ __forceinline__ N pm(N a, N b)
 {
 	if constexpr (std::is_same<N, SD>::value) return SD(se_mul(a.v, b.v));
