@@ -353,7 +353,7 @@ PRECISION_SHAPE = (1024, 512, 512)
 def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt", "uxx1")):
     """The stencils advanced nsteps time steps from a Gaussian pulse (sigma 16
     cells) + 1e-3 noise with stable coefficients, in FP64 (strict), FP64 with
-    float-float arithmetic, FP64 state with FP32 increments (uxx1), and FP32
+    float-float arithmetic, FP64 state with FP32 increments (KG_F64_MIX), and FP32
     and BF16 storage with FP32 arithmetic, side by side.  Every `every` steps the
     newest level of each narrow form is compared with FP64's (max and RMS of
     the difference relative to max and RMS of the FP64 field) and its FP64
@@ -371,8 +371,7 @@ def run_precision(shape=PRECISION_SHAPE, nsteps=100, every=10, names=("wave13pt"
                  ("f32", kgb200.KG_F32, torch.float32), ("bf16", kgb200.KG_BF16, torch.bfloat16)]
     out = {}
     for name in names:
-        # the FP64-state / FP32-increment form is uxx1's (an incremental update)
-        forms = [f for f in all_forms if f[0] != "f64mix" or name == "uxx1"]
+        forms = all_forms
         inputs = make_inputs([name], variant=3, shape=shape)
         coef, arrs, _ = inputs[name]
         f64 = [torch.from_numpy(a).to("cuda") for a in arrs]
@@ -1017,7 +1016,7 @@ def main():
     if not args.no_forms:
         line["forms"] = {"fp64_float_float": ff_form, "precision_sweep": dict(
             workload="wave13pt and uxx1, 1024x512x512, 100 steps from a Gaussian pulse (sigma 16) + 1e-3 noise; "
-                     "FP64 strict vs float-float (f64ff), FP64 state with FP32 increments (f64mix, uxx1), FP32 and "
+                     "FP64 strict vs float-float (f64ff), FP64 state with FP32 increments (f64mix), FP32 and "
                      "BF16 storage (FP32 arithmetic); errors relative to FP64 every 10 steps",
             **run_precision())}
         line["forms"]["batched"] = run_batched(tune_cache=os.environ.get("KG_TUNE_CACHE"))

@@ -54,10 +54,12 @@ typedef enum {
 	KG_F64_FF = 6,   /* FP64 storage; arithmetic on float-float pairs (hi+lo
 	                    FP32 with error-free transformations) on the FP32 pipes:
 	                    ~1e-14 of FP64 normwise, values within FP32's range    */
-	KG_F64_MIX = 7   /* FP64 storage; each step's increment in FP32 arithmetic,
-	                    added to the FP64 state in FP64 (uxx1 only: the state
-	                    keeps FP64 precision, a step errs by FP32's relative
-	                    error of its increment)                                */
+	KG_F64_MIX = 7   /* FP64 storage; the update's small part in FP32
+	                    arithmetic, combined with the FP64 state in FP64 (uxx1:
+	                    its increment; wave13pt: its neighbour differences from
+	                    the centre): the state keeps FP64 precision, a step errs
+	                    by FP32's relative error of that part.  uxx1 and
+	                    wave13pt only                                          */
 } kg_dtype;
 
 /* Stencil ids (the suite's test directories). */

@@ -84,8 +84,8 @@ static kg_status validate(const kg_problem* p)
 	if (p->stencil < 0 || p->stencil >= KG_NSTENCILS) return fail(KG_EINVAL, "unknown stencil %d", p->stencil);
 	const Meta& m = k_meta[p->stencil];
 	if (p->dtype < KG_F64 || p->dtype > KG_F64_MIX) return fail(KG_EINVAL, "%s: unknown dtype %d", m.name, p->dtype);
-	if (p->dtype == KG_F64_MIX && p->stencil != KG_UXX1)
-		return fail(KG_ENOTSUP, "%s: the FP64-state / FP32-increment form is provided for uxx1 only", m.name);
+	if (p->dtype == KG_F64_MIX && p->stencil != KG_UXX1 && p->stencil != KG_WAVE13PT)
+		return fail(KG_ENOTSUP, "%s: the FP64-state / FP32-increment form is provided for uxx1 and wave13pt", m.name);
 	if (p->dtype == KG_U8 && p->stencil != KG_GAMEOFLIFE)
 		return fail(KG_ENOTSUP, "%s: byte cells are provided for gameoflife only", m.name);
 	if (p->nx < 0 || p->ny < 0 || p->ns < 0) return fail(KG_EINVAL, "%s: negative size", m.name);
@@ -126,7 +126,7 @@ static cudaError_t dispatch(const kg_problem& p, cudaStream_t st)
 	case KG_BF16: return sweep_bf16(p, st);
 	case KG_F16: return sweep_f16(p, st);
 	case KG_U8: return sweep_u8(p, st);
-	case KG_F64_MIX: return sweep_uxx1_mix(p, st);
+	case KG_F64_MIX: return p.stencil == KG_WAVE13PT ? sweep_wave13pt_mix(p, st) : sweep_uxx1_mix(p, st);
 	default: return cudaErrorInvalidValue;
 	}
 }
@@ -291,8 +291,9 @@ kg_status kg_kernel_regcount(int stencil, kg_dtype dt, int* nregs)
 		e = regs_u8(p, nregs);
 		break;
 	case KG_F64_MIX:
-		if (stencil != KG_UXX1) return fail(KG_ENOTSUP, "the FP64-state / FP32-increment form: uxx1 only");
-		e = regs_uxx1_mix(nregs);
+		if (stencil != KG_UXX1 && stencil != KG_WAVE13PT)
+			return fail(KG_ENOTSUP, "the FP64-state / FP32-increment form: uxx1 and wave13pt");
+		e = stencil == KG_WAVE13PT ? regs_wave13pt_mix(nregs) : regs_uxx1_mix(nregs);
 		break;
 	default: return fail(KG_EINVAL, "kg_kernel_regcount: unknown dtype");
 	}

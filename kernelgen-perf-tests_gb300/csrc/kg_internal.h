@@ -20,6 +20,8 @@ cudaError_t regs_f64(const kg_problem& p, int* nregs);
 cudaError_t regs_f64fma(const kg_problem& p, int* nregs);
 cudaError_t regs_f64ff(const kg_problem& p, int* nregs);
 cudaError_t sweep_uxx1_mix(const kg_problem& p, cudaStream_t s);
+cudaError_t sweep_wave13pt_mix(const kg_problem& p, cudaStream_t s);
+cudaError_t regs_wave13pt_mix(int* nregs);
 cudaError_t regs_uxx1_mix(int* nregs);
 cudaError_t regs_f32(const kg_problem& p, int* nregs);
 cudaError_t regs_bf16(const kg_problem& p, int* nregs);

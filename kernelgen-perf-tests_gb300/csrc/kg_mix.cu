@@ -1,5 +1,6 @@
-// kg_uxx1_mix.cu -- uxx1 in the KG_F64_MIX form: FP64 state, the update's
-// increment in FP32 arithmetic, added to the state in FP64.
+// kg_mix.cu -- the KG_F64_MIX form of the incremental updates, uxx1 and
+// wave13pt: FP64 state, the update's small part in FP32 arithmetic, combined
+// with the state in FP64.
 //
 // uxx1 advances u by an increment each step (uxx1/uxx1.c:83-106):
 //   u1 = u0 + (dth / d) * (c1 (xx - xx[x-1]) + c2 (xx[x+1] - xx[x-2]) + ...y, z)
@@ -13,6 +14,15 @@
 // enter FP32 truncated to 24 significant bits by integer operations (the
 // conversion instruction would issue to the FP64 unit); the increment goes
 // back to FP64 by exact widening, also from its bit fields.
+//
+// wave13pt (wave13pt/wave13pt.c:640-651) is rewritten around the centre value
+// c = w1[i]: w2 = (m0 + 6 m1 + 6 m2) c - w0 + m1 D1 + m2 D2, with D1, D2 the
+// sums of the differences w1[neighbour] - c over the six neighbours at
+// distance 1 and 2.  The differences are formed in FP32 from the float-float
+// split of each value (hi parts subtract exactly when the values are within a
+// factor of two, the low parts add the rest), so they carry FP32's relative
+// error of the difference, not of w; m1 D1 + m2 D2 is FP32 and the rest one
+// FP64 FMA and one addition.
 #include <cstdint>
 
 #include "kg_internal.h"
@@ -115,6 +125,94 @@ __global__ void __launch_bounds__(kMixBX * kMixBY) uxx1_mix_kernel(int nx, int n
 	}
 }
 
+// ---- wave13pt ------------------------------------------------------------
+
+constexpr int kWmBX = 32, kWmBY = 8, kWmKC = 16;
+
+struct WavePlane {
+	double x1, xm1, x2, xm2, y1, ym1, y2, ym2, z2, w0;
+};
+
+__device__ __forceinline__ WavePlane wave_load(long long c, long long sy, long long sz,
+	const double* __restrict__ w0, const double* __restrict__ w1)
+{
+	WavePlane p;
+	p.x1 = __ldg(w1 + c + 1);
+	p.xm1 = __ldg(w1 + c - 1);
+	p.x2 = __ldg(w1 + c + 2);
+	p.xm2 = __ldg(w1 + c - 2);
+	p.y1 = __ldg(w1 + c + sy);
+	p.ym1 = __ldg(w1 + c - sy);
+	p.y2 = __ldg(w1 + c + 2 * sy);
+	p.ym2 = __ldg(w1 + c - 2 * sy);
+	p.z2 = __ldg(w1 + c + 2 * sz);
+	p.w0 = __ldg(w0 + c);
+	return p;
+}
+
+// (a - c) + (b - c) + ... for float-float values against the centre (hi, lo)
+__device__ __forceinline__ float wave_diffs(FF2 c, FF2 a, FF2 b, FF2 d, FF2 e, FF2 f, FF2 g)
+{
+	const float h = (((((a.hi - c.hi) + (b.hi - c.hi)) + (d.hi - c.hi)) + (e.hi - c.hi)) + (f.hi - c.hi)) + (g.hi - c.hi);
+	const float l = (a.lo + b.lo + d.lo + e.lo + f.lo + g.lo) - 6.0f * c.lo;
+	return h + l;
+}
+
+// One thread per (i, j) column, kWmKC planes of it, the next plane's loads in
+// flight; arrays in the reference's argument order: w0, w1, w2.
+__global__ void __launch_bounds__(kWmBX * kWmBY) wave13pt_mix_kernel(int nx, int ny, int ns, double M, float m1,
+	float m2, const double* __restrict__ w0, const double* __restrict__ w1, double* __restrict__ w2)
+{
+	const int i = 2 + blockIdx.x * kWmBX + threadIdx.x;
+	if (i >= nx - 2) return;
+	const long long sy = nx, sz = (long long)nx * ny;
+	const int tyn = (ny - 4 + kWmBY - 1) / kWmBY, tzn = (ns - 4 + kWmKC - 1) / kWmKC;
+	for (int ty = blockIdx.y; ty < tyn; ty += gridDim.y) {
+		const int j = 2 + ty * kWmBY + threadIdx.y;
+		if (j >= ny - 2) continue;
+		for (int tz = blockIdx.z; tz < tzn; tz += gridDim.z) {
+			const int k0 = 2 + tz * kWmKC, k1 = min(k0 + kWmKC, ns - 2);
+			long long c = i + sy * j + sz * k0;
+			// the column of w1, planes k-2 .. k+1 (raw centre, split pairs)
+			FF2 zm2 = ff2_from_double(__ldg(w1 + c - 2 * sz)), zm1 = ff2_from_double(__ldg(w1 + c - sz));
+			double zc = __ldg(w1 + c), zc1 = __ldg(w1 + c + sz);
+			FF2 z0 = ff2_from_double(zc), zp1 = ff2_from_double(zc1);
+			WavePlane cur = wave_load(c, sy, sz, w0, w1);
+			for (int k = k0; k < k1; k++, c += sz) {
+				WavePlane nxt = cur;
+				if (k + 1 < k1) nxt = wave_load(c + sz, sy, sz, w0, w1);
+				const FF2 zp2 = ff2_from_double(cur.z2);
+				const float d1 = wave_diffs(z0, ff2_from_double(cur.x1), ff2_from_double(cur.xm1), ff2_from_double(cur.y1),
+					ff2_from_double(cur.ym1), zp1, zm1);
+				const float d2 = wave_diffs(z0, ff2_from_double(cur.x2), ff2_from_double(cur.xm2), ff2_from_double(cur.y2),
+					ff2_from_double(cur.ym2), zp2, zm2);
+				const float inc = m1 * d1 + m2 * d2;
+				w2[c] = __dadd_rn(__fma_rn(M, zc, -cur.w0), mix_f64(inc));
+				// the column moves one plane on
+				zm2 = zm1;
+				zm1 = z0;
+				z0 = zp1;
+				zp1 = zp2;
+				zc = zc1;
+				zc1 = cur.z2;
+				cur = nxt;
+			}
+		}
+	}
+}
+
+cudaError_t sweep_wave13pt_mix(const kg_problem& p, cudaStream_t st)
+{
+	if (p.nx < 5 || p.ny < 5 || p.ns < 5) return cudaSuccess;   // empty domain [2, n-3]
+	const int tx = (p.nx - 4 + kWmBX - 1) / kWmBX, ty = (p.ny - 4 + kWmBY - 1) / kWmBY,
+		tz = (p.ns - 4 + kWmKC - 1) / kWmKC;
+	dim3 grid(tx, (unsigned)std::min(ty, 65535), (unsigned)std::min(tz, 65535));
+	const double m0 = p.coef[0], m1 = p.coef[1], m2 = p.coef[2];
+	wave13pt_mix_kernel<<<grid, dim3(kWmBX, kWmBY), 0, st>>>(p.nx, p.ny, p.ns, m0 + 6.0 * m1 + 6.0 * m2, (float)m1,
+		(float)m2, (const double*)p.arr[0], (const double*)p.arr[1], (double*)p.arr[2]);
+	return cudaGetLastError();
+}
+
 cudaError_t sweep_uxx1_mix(const kg_problem& p, cudaStream_t st)
 {
 	if (p.nx < 4 || p.ny < 4 || p.ns < 4) return cudaSuccess;   // empty domain [2, n-2]
@@ -131,6 +229,14 @@ cudaError_t regs_uxx1_mix(int* nregs)
 {
 	cudaFuncAttributes a;
 	cudaError_t e = cudaFuncGetAttributes(&a, (const void*)uxx1_mix_kernel);
+	if (e == cudaSuccess) *nregs = a.numRegs;
+	return e;
+}
+
+cudaError_t regs_wave13pt_mix(int* nregs)
+{
+	cudaFuncAttributes a;
+	cudaError_t e = cudaFuncGetAttributes(&a, (const void*)wave13pt_mix_kernel);
 	if (e == cudaSuccess) *nregs = a.numRegs;
 	return e;
 }

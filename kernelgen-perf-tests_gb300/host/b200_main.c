@@ -8,8 +8,8 @@
  *
  * Knobs (environment, set by the target makefile from make variables):
  *   B200_PREC  fp64 (default; bitwise = IEEE reference) | fp64fma | fp64ff
- *              (FP64 storage, float-float arithmetic) | fp64mix (uxx1: FP64
- *              state, FP32 increments) | fp32 | bf16 | fp16 |
+ *              (FP64 storage, float-float arithmetic) | fp64mix (uxx1,
+ *              wave13pt: FP64 state, FP32 increments) | fp32 | bf16 | fp16 |
  *              u8 (gameoflife on 0/1 byte cells)
  *   B200_INIT  reference (default) | bernoulli | unit | pulse
  *   B200_MODE  plain (default: one launch per sweep, timed) | graph (the
