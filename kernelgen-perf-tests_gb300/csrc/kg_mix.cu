@@ -127,6 +127,23 @@ __global__ void __launch_bounds__(kMixBX * kMixBY) uxx1_mix_kernel(int nx, int n
 
 // ---- wave13pt ------------------------------------------------------------
 
+// x as a float pair: hi = x truncated to 24 significant bits (mix_f32), lo =
+// the remaining 29 bits rounded to FP32 (one integer-to-float conversion,
+// which issues to the otherwise idle XU pipe, scaled by 2^(e-1075)).  Values
+// outside FP32's normal range keep only hi, as ff2_from_double does.
+__device__ __forceinline__ FF2 mix_split(double x)
+{
+	const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+	const unsigned bh = (unsigned)(b >> 32), bl = (unsigned)b;
+	const int e = (int)((bh >> 20) & 0x7ff);
+	const float hi = mix_f32(x);
+	if (e < 949 || e > 1150) return FF2(hi, 0.f);
+	const float scale = __uint_as_float((unsigned)(e - 948) << 23);   // 2^(e - 1075)
+	const float lo = __uint_as_float(__float_as_uint(__fmul_rn(__uint2float_rn(bl & 0x1fffffffu), scale)) |
+		(bh & 0x80000000u));
+	return FF2(hi, lo);
+}
+
 constexpr int kWmBX = 32, kWmBY = 8, kWmKC = 16;
 
 struct WavePlane {
@@ -174,18 +191,18 @@ __global__ void __launch_bounds__(kWmBX * kWmBY) wave13pt_mix_kernel(int nx, int
 			const int k0 = 2 + tz * kWmKC, k1 = min(k0 + kWmKC, ns - 2);
 			long long c = i + sy * j + sz * k0;
 			// the column of w1, planes k-2 .. k+1 (raw centre, split pairs)
-			FF2 zm2 = ff2_from_double(__ldg(w1 + c - 2 * sz)), zm1 = ff2_from_double(__ldg(w1 + c - sz));
+			FF2 zm2 = mix_split(__ldg(w1 + c - 2 * sz)), zm1 = mix_split(__ldg(w1 + c - sz));
 			double zc = __ldg(w1 + c), zc1 = __ldg(w1 + c + sz);
-			FF2 z0 = ff2_from_double(zc), zp1 = ff2_from_double(zc1);
+			FF2 z0 = mix_split(zc), zp1 = mix_split(zc1);
 			WavePlane cur = wave_load(c, sy, sz, w0, w1);
 			for (int k = k0; k < k1; k++, c += sz) {
 				WavePlane nxt = cur;
 				if (k + 1 < k1) nxt = wave_load(c + sz, sy, sz, w0, w1);
-				const FF2 zp2 = ff2_from_double(cur.z2);
-				const float d1 = wave_diffs(z0, ff2_from_double(cur.x1), ff2_from_double(cur.xm1), ff2_from_double(cur.y1),
-					ff2_from_double(cur.ym1), zp1, zm1);
-				const float d2 = wave_diffs(z0, ff2_from_double(cur.x2), ff2_from_double(cur.xm2), ff2_from_double(cur.y2),
-					ff2_from_double(cur.ym2), zp2, zm2);
+				const FF2 zp2 = mix_split(cur.z2);
+				const float d1 = wave_diffs(z0, mix_split(cur.x1), mix_split(cur.xm1), mix_split(cur.y1),
+					mix_split(cur.ym1), zp1, zm1);
+				const float d2 = wave_diffs(z0, mix_split(cur.x2), mix_split(cur.xm2), mix_split(cur.y2),
+					mix_split(cur.ym2), zp2, zm2);
 				const float inc = m1 * d1 + m2 * d2;
 				w2[c] = __dadd_rn(__fma_rn(M, zc, -cur.w0), mix_f64(inc));
 				// the column moves one plane on
