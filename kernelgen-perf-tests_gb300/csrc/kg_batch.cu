@@ -29,6 +29,8 @@
 
 #include <algorithm>
 
+// the batch's small tiles are latency-bound: every sum on the FP64 unit
+#define KG_SUMS_ON_FP64_UNIT 1
 #include "kg_engine.cuh"
 #include "kg_internal.h"
 

@@ -69,10 +69,17 @@ template <class N> __device__ __forceinline__ N pdiv(N a, N b)
 // 8-term sum 2 (1.209), lapgsrb's 12-term sum 3 and gameoflife's 3 slower): a
 // sum's chain shares the FP64 unit with the integer pipes, which also form the
 // products.
+// A translation unit whose sweeps are bound by load latency rather than by the
+// FP64 unit (the batch's small tiles) defines KG_SUMS_ON_FP64_UNIT: the
+// integer additions' longer latency would then cost more than they save
+// (256-problem FP64 batch: 40.9 -> 32.9 Gpts/s with them).
+#ifndef KG_SUMS_ON_FP64_UNIT
+#define KG_SUMS_ON_FP64_UNIT 0
+#endif
 template <int I, int K> __device__ __forceinline__ double nsum_sd(double acc) { return acc; }
 template <int I, int K, class... T> __device__ __forceinline__ double nsum_sd(double acc, SD x, T... rest)
 {
-	if constexpr (I < K) acc = se_add(acc, x.v);
+	if constexpr (I < K && !KG_SUMS_ON_FP64_UNIT) acc = se_add(acc, x.v);
 	else acc = __dadd_rn(acc, x.v);
 	return nsum_sd<I + 1, K>(acc, rest...);
 }
