@@ -1,7 +1,7 @@
 /*
  * kg_oracle.c -- CPU restatement of the kernelgen-perf-tests stencil sweeps.
  *
- * TEST INFRASTRUCTURE ONLY (the checker; see kg_oracle.h).  Built twice by
+ * TEST INFRASTRUCTURE ONLY (the oracle; see kg_oracle.h).  Built twice by
  * oracle/Makefile: strict (-O2 -ffp-contract=off: the bitwise oracle) and
  * with the suite's fast-math flags plus OpenMP (the timed CPU baseline).
  *

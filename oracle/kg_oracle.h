@@ -1,7 +1,7 @@
 /*
  * kg_oracle.h -- CPU restatement of the kernelgen-perf-tests stencil sweeps.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: tests, the smoke
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: tests, the smoke
  * check and the CPU-baseline leg of bench.py call it; the product (the
  * sm_103a library and the b200 host drivers) never links or calls it.
  *

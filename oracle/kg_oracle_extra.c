@@ -2,7 +2,7 @@
  * kg_oracle_extra.c -- CPU restatement of the suite's tests that are not
  * stencil sweeps: vecadd, matvec, matmul, sincos, whispering.
  *
- * TEST INFRASTRUCTURE ONLY (the checker), like kg_oracle.c.  Each kernel
+ * TEST INFRASTRUCTURE ONLY (the oracle), like kg_oracle.c.  Each kernel
  * follows the reference loop and expression in order; each *_program
  * reproduces the reference main(): rand() draws in its order (the reference
  * never seeds: srand(1)), the time loop with its pointer rotation, and the

@@ -1,7 +1,7 @@
 """ctypes binding of the oracle (oracle/kg_oracle.c): test infrastructure.
 
-The oracle is the checker.  Only tests, the smoke check and bench.py's CPU
-baseline leg use it.
+Only tests, the smoke check and bench.py's CPU baseline leg use the oracle;
+the product never does.
 """
 import ctypes
 import os

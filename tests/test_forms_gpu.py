@@ -119,8 +119,8 @@ FF_NAMES = [n for n in kgb200.STENCILS if n != "gameoflife"]
 
 @pytest.mark.parametrize("name", FF_NAMES)
 def test_float_float_form_within_1e12(name):
-    """KG_F64_FF (FP64 storage, float-float arithmetic) stays within the
-    spec FP64 tolerance of the oracle (measured ~1e-14)."""
+    """KG_F64_FF (FP64 storage, float-float arithmetic) stays within the FP64
+    drop-in's tolerance of the oracle, 1e-12 normwise (measured ~1e-14)."""
     from test_parity_gpu import gpu_run, normwise
     shape = (129, 300) if name in kgb200.IS2D else (64, 32, 32)
     case = ol.Case(name, shape)
