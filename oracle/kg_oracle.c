@@ -14,6 +14,9 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define IX(i, j, k) ((size_t)(i) + (size_t)nx * ((size_t)(j) + (size_t)ny * (size_t)(k)))
 #define IX2(i, j) ((size_t)(i) + (size_t)nx * (size_t)(j))
@@ -262,6 +265,16 @@ void or_conway_u8(int nx, int ny, const uint8_t* u0, uint8_t* u1)
 
 static const int k_narr[OR_NTESTS] = { 2, 4, 4, 6, 3, 5, 5, 2, 2, 2, 2 };
 static const int k_ncoef[OR_NTESTS] = { 2, 3, 3, 2, 3, 0, 0, 3, 4, 6, 0 };
+
+/* Threads of the OpenMP loops (the suite's gcc target itself is serial). */
+void or_set_threads(int n)
+{
+#ifdef _OPENMP
+	if (n > 0) omp_set_num_threads(n);
+#else
+	(void)n;
+#endif
+}
 
 int or_narrays(int test) { return (test >= 0 && test < OR_NTESTS) ? k_narr[test] : -1; }
 int or_ncoefs(int test) { return (test >= 0 && test < OR_NTESTS) ? k_ncoef[test] : -1; }

@@ -94,6 +94,8 @@ void or_init_bernoulli_u8(int n, uint8_t* u0, uint8_t* u1, double p, unsigned se
 
 /* One sweep with the current array roles. */
 void or_sweep(or_case* c);
+/* Threads of the OpenMP loops of the fast build (no effect on the strict build). */
+void or_set_threads(int n);
 /* nt sweeps with the reference's pointer rotation after each sweep. */
 void or_run(or_case* c, int nt);
 

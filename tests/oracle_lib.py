@@ -43,6 +43,8 @@ def load(flavour="strict"):
     lib = ctypes.CDLL(path)
     lib.or_init.argtypes = [ctypes.POINTER(OrCase), ctypes.c_int, ctypes.c_uint]
     lib.or_sweep.argtypes = [ctypes.POINTER(OrCase)]
+    lib.or_set_threads.argtypes = [ctypes.c_int]
+    lib.or_set_threads.restype = None
     lib.or_run.argtypes = [ctypes.POINTER(OrCase), ctypes.c_int]
     lib.or_initial_mean.argtypes = [ctypes.POINTER(OrCase)]
     lib.or_initial_mean.restype = ctypes.c_double
