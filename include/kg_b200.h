@@ -168,8 +168,10 @@ kg_status kg_extra_regcount(const char* name, kg_dtype dt, int* nregs);
  * (and KG_F32 wave13pt) where every array and row starts on a 16-byte
  * boundary, else DIRECT; DIRECT for KG_F64/KG_F64_FMA; STAGED for KG_F64_FF
  * (TMA for its divergence and uxx1 where aligned).  Built: DIRECT and TMA
- * for every floating type but KG_F64_FF; STAGED and TMA for KG_F64_FF; DIRECT
- * for KG_U8.  The engines evaluate the same expressions in the same order (the
+ * for every floating type but KG_F64_FF and KG_F64_MIX; STAGED and TMA for
+ * KG_F64_FF; DIRECT for KG_F64_MIX and KG_U8.  Grids of tiles beyond the launch
+ * limits are taken in turn.  The engines evaluate the same expressions in the
+ * same order (the
  * tests check their outputs equal bit for bit).  TMA needs 16-byte aligned
  * arrays and rows. */
 typedef enum {
