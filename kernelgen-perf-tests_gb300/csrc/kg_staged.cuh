@@ -279,11 +279,16 @@ struct StagedLaunch {
 		constexpr size_t bytes = smem();
 		static_assert(bytes <= 200 * 1024, "halo tiles exceed shared memory");
 		if (bytes > 48 * 1024) {
-			static bool once = false;
-			if (!once) {
-				cudaError_t e = cudaFuncSetAttribute(func(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+			// the opt-in is a per-device setting of the function: once per device
+			static bool set_on[64];
+			int dev = 0;
+			cudaError_t e = cudaGetDevice(&dev);
+			if (e != cudaSuccess) return e;
+			if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+			if (!set_on[dev]) {
+				e = cudaFuncSetAttribute(func(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 				if (e != cudaSuccess) return e;
-				once = true;
+				set_on[dev] = true;
 			}
 		}
 		K kop;
