@@ -201,8 +201,21 @@ kg_status kg_sweep(const kg_problem* p, kg_stream_t stream);
 
 /* Waits for `stream`, then reports whether a TMA-engine sweep since the last
  * call gave up waiting for its tile copies (KG_ETIMEOUT: that sweep's output
- * is incomplete) and clears the record.  No counterpart in the reference. */
+ * is incomplete) and clears the record.  The record is one flag per device,
+ * shared by every stream; its device address is looked up once per device
+ * (do not use the library across cudaDeviceReset).  No counterpart in the
+ * reference. */
 kg_status kg_engine_status(kg_stream_t stream);
+
+/* How long (GPU clock cycles) a TMA-engine compute warp waits for a step's
+ * tile copies before it gives up, for kernels launched after the call
+ * (plans and batches keep the limit they were recorded with).  Negative:
+ * the default, 2^31 cycles (about 1 s).  0: give up unless the copies have
+ * already landed when the warp first looks -- a way to make the failure
+ * path run without a fault, for tests.  Whatever the limit, a CTA that
+ * gives up waits for every copy it issued before it exits.  Process-wide.
+ * No counterpart in the reference. */
+kg_status kg_set_tma_wait_limit(long long cycles);
 
 /* ---- checksums (the reference's "initial mean" / "final mean") ---------- */
 
@@ -222,7 +235,12 @@ kg_status kg_checksum(kg_dtype dt, size_t n, int narr, const void* const* arrays
  * KG_CHECKSUM_NOALLOC_PARTIALS doubles (16 KiB) that every GPU loading the
  * library keeps until the process exits; n above KG_CHECKSUM_NOALLOC_MAX_N
  * is rejected with KG_EINVAL.  The first call on each device looks up the
- * array's device address (make it before any stream capture).  All calls
+ * array's device address (make it before any stream capture), and with
+ * CUDA's lazy module loading the first launch of each storage type's two
+ * kernels loads them, which may itself take device memory and synchronise:
+ * make one call per device and storage type at start-up, before the phase
+ * that must not allocate.  The cached address does not survive
+ * cudaDeviceReset: do not use the library across a device reset.  All calls
  * share the array: calls whose kernels may overlap on the GPU (different
  * streams without ordering) race and must be serialised by the caller.
  * No counterpart in the reference. */

@@ -176,6 +176,8 @@ kg_status kg_program_run(kg_problem* p, int nt, int copy_back_mask, kg_timings* 
 	if (made == nev) cudaEventRecord(*free1, st);
 	const kg_status sync = fail_cuda(cudaStreamSynchronize(st), "kg_program_run");
 	if (s == KG_OK) s = sync;
+	// a TMA-engine sweep whose bounded wait gave up left its output incomplete
+	if (s == KG_OK && ran) s = kg_engine_status(stream);
 	if (s == KG_OK) {
 		float ms = 0;
 		cudaEventElapsedTime(&ms, *load0, *load1);

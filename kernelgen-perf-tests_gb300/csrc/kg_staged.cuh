@@ -15,6 +15,8 @@
 // Inputs read only at the point itself come straight from global memory.
 #pragma once
 
+#include <atomic>
+
 #include "kg_engine.cuh"
 
 namespace kg {
@@ -279,16 +281,18 @@ struct StagedLaunch {
 		constexpr size_t bytes = smem();
 		static_assert(bytes <= 200 * 1024, "halo tiles exceed shared memory");
 		if (bytes > 48 * 1024) {
-			// the opt-in is a per-device setting of the function: once per device
-			static bool set_on[64];
+			// the opt-in is a per-device setting of the function: once per
+			// device (host threads may race to set it; setting it twice is
+			// harmless, and the flag itself is atomic)
+			static std::atomic<bool> set_on[64];
 			int dev = 0;
 			cudaError_t e = cudaGetDevice(&dev);
 			if (e != cudaSuccess) return e;
 			if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-			if (!set_on[dev]) {
+			if (!set_on[dev].load(std::memory_order_acquire)) {
 				e = cudaFuncSetAttribute(func(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 				if (e != cudaSuccess) return e;
-				set_on[dev] = true;
+				set_on[dev].store(true, std::memory_order_release);
 			}
 		}
 		K kop;

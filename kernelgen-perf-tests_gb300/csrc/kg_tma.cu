@@ -2,15 +2,27 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <cstring>
 #include <mutex>
 
 #include "kg_internal.h"
+#include "kg_tma.cuh"
 
 namespace kg {
 
 // Raised (set to 1) by a TMA-engine kernel whose wait for a copy gave up.
 static __device__ int g_tma_error;
+
+// The compute warps' wait limit passed to kernels launched from now on
+// (process-wide; negative: the default).
+static std::atomic<long long> g_tma_wait{-1};
+
+long long tma_wait_limit()
+{
+	const long long w = g_tma_wait.load(std::memory_order_relaxed);
+	return w < 0 ? kTmaWaitCycles : w;
+}
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn(cudaError_t* err)
 {
@@ -46,6 +58,8 @@ cudaError_t tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, const void
 	return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// The device address of g_tma_error on the current device, looked up once per
+// device and cached (it does not survive cudaDeviceReset).
 int* tma_error_flag()
 {
 	static std::mutex m;
@@ -64,6 +78,13 @@ int* tma_error_flag()
 }  // namespace kg
 
 using namespace kg;
+
+extern "C" kg_status kg_set_tma_wait_limit(long long cycles)
+{
+	clear_error();
+	g_tma_wait.store(cycles < 0 ? -1 : cycles, std::memory_order_relaxed);
+	return KG_OK;
+}
 
 extern "C" kg_status kg_engine_status(kg_stream_t stream)
 {

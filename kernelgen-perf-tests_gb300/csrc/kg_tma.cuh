@@ -23,10 +23,15 @@
 // domain point lies inside the array.  Inputs read only at the point itself
 // are not staged: each thread loads them from global memory.
 //
-// Waits are bounded: a wait that runs past kTmaWaitCycles records an error in
-// a device flag (read back by kg_engine_status) and the warp returns; the
-// producer first waits once more, with the same bound, for the copies it
-// issued.
+// Waits are bounded.  A compute warp waits for a step's copies at most
+// `wait` clock cycles (a kernel argument: kTmaWaitCycles unless the host set
+// another limit, kg_set_tma_wait_limit; 0 = give up unless the copies have
+// already landed at the first look); when that runs out it records an error
+// in a device flag (read back by kg_engine_status), raises the CTA's abort
+// flag in shared memory and returns.  The producer waits for the compute
+// warps at most kTmaWaitCycles and stops issuing as soon as the abort flag is
+// up; either way it then waits, again at most kTmaWaitCycles, for every copy
+// it issued to land before the CTA exits.
 #pragma once
 
 #include <cuda.h>
@@ -74,14 +79,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 	return done != 0;
 }
 
-// Wait for the phase with the given parity to complete, for at most
-// kTmaWaitCycles; false if the bound ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// Whether the phase with the given parity has completed, without waiting.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity)
 {
+	uint32_t done;
+	asm volatile(
+		"{\n\t.reg .pred p;\n\t"
+		"mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		"selp.u32 %0, 1, 0, p;\n\t}"
+		: "=r"(done)
+		: "r"(smem_addr(bar)), "r"(parity)
+		: "memory");
+	return done != 0;
+}
+
+// Wait for the phase with the given parity to complete, for at most `limit`
+// clock cycles (0: only look once), and no longer once *abort (if given) is
+// set; false if it did not complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit,
+	const volatile int* abort = nullptr)
+{
+	if (limit <= 0) return mbar_test_wait(bar, parity);
 	if (mbar_try_wait(bar, parity)) return true;
 	const long long t0 = clock64();
-	while (!mbar_try_wait(bar, parity))
-		if (clock64() - t0 > kTmaWaitCycles) return false;
+	while (!mbar_try_wait(bar, parity)) {
+		if (abort && *abort) return false;
+		if (clock64() - t0 > limit) return false;
+	}
 	return true;
 }
 
@@ -152,7 +176,8 @@ template <class Op, class S, int BX, int BY, int L> struct TGeo {
 	static constexpr int box_bytes(int q) { return staged(q) ? W(q) * H(q) * ES : 0; }
 	static constexpr int PS(int q) { return round_up(box_bytes(q), 128); }   // plane stride, bytes
 	static constexpr int NB = L + 1;                                         // steps in flight
-	static constexpr int kBar = 128;                                         // 2 x NB mbarriers
+	static constexpr int kBar = 128;                          // 2 x NB mbarriers, then the abort flag
+	static constexpr int kAbort = kBar - 8;
 	static constexpr int offset(int q) { int o = kBar; for (int r = 0; r < q; r++) o += R(r) * PS(r); return o; }
 	static constexpr int total() { return offset(NIN); }
 	static constexpr int step_bytes() { int b = 0; for (int q = 0; q < NIN; q++) b += box_bytes(q); return b; }
@@ -161,7 +186,7 @@ template <class Op, class S, int BX, int BY, int L> struct TGeo {
 	static constexpr bool fits() {
 		for (int q = 0; q < NIN; q++)
 			if (Op::halo(q).x0 > A || W(q) > 256 || H(q) > 256) return false;
-		return L >= 1 && 2 * NB * 8 <= kBar && step_bytes() > 0;
+		return L >= 1 && 2 * NB * 8 <= kAbort && step_bytes() > 0;
 	}
 };
 
@@ -221,7 +246,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 // ahead of the compute warps, which never wait for each other.
 template <class Op, class N, class S, int TX, int TY, int PY, int L>
 __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, const __grid_constant__ TMaps maps,
-	int nx, int ny, int ns, int kc, int yt0, int* err)
+	int nx, int ny, int ns, int kc, int yt0, int* err, long long wait)
 {
 	constexpr int BX = TX, BY = TY * PY, NC = TX * TY;
 	using G = TGeo<Op, S, BX, BY, L>;
@@ -236,6 +261,7 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 	extern __shared__ __align__(128) unsigned char sm[];
 	uint64_t* full = reinterpret_cast<uint64_t*>(sm);
 	uint64_t* done = full + NB;
+	volatile int* abort = reinterpret_cast<volatile int*>(sm + G::kAbort);
 
 	const int tid = threadIdx.x;
 	const int xt = blockIdx.x * BX, yt = Op::LY + (yt0 + (int)blockIdx.y) * BY;
@@ -246,6 +272,7 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 			mbar_init(&full[b], 1);
 			mbar_init(&done[b], NC / 32);
 		}
+		*abort = 0;
 		mbar_fence_init();
 	}
 	__syncthreads();
@@ -261,10 +288,10 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 		for (int kb = Op::LZ + blockIdx.z * kc; kb < kend && ok; kb += gridDim.z * kc) {
 			const int nsteps = min(kc, kend - kb);
 			// a new run's window may reuse any slot: wait for the previous run
-			if (g > 0) ok = mbar_wait(&done[(g - 1) % NB], ((g - 1) / NB) & 1);
+			if (g > 0) ok = mbar_wait(&done[(g - 1) % NB], ((g - 1) / NB) & 1, kTmaWaitCycles, abort);
 			for (int t = 0; t < nsteps && ok; t++) {
 				const uint32_t gt = g + t;
-				if (t >= L + 1) ok = mbar_wait(&done[(gt - L - 1) % NB], ((gt - L - 1) / NB) & 1);
+				if (t >= L + 1) ok = mbar_wait(&done[(gt - L - 1) % NB], ((gt - L - 1) / NB) & 1, kTmaWaitCycles, abort);
 				if (!ok) break;
 				fence_proxy_async();
 				tma_issue<Op, S, G>(maps, sm, &full[gt % NB], xt, yt, kb + t, t == 0);
@@ -272,11 +299,16 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 			}
 			g += nsteps;
 		}
+		// stay until the compute warps are done with the last step, or gave up
+		if (ok && issued > 0) ok = mbar_wait(&done[(issued - 1) % NB], ((issued - 1) / NB) & 1, kTmaWaitCycles, abort);
 		if (!ok) {
 			atomicExch(err, 1);
-			// the copies already issued land before the CTA's shared memory goes away
+			// Every step before the last NB issued is done (the copies of step
+			// w + NB were issued only after step w was done): the copies still
+			// in flight belong to those NB steps, and they land before the
+			// CTA's shared memory goes away.
 			for (uint32_t w = issued > NB ? issued - NB : 0; w < issued; w++)
-				mbar_wait(&full[w % NB], (w / NB) & 1);
+				mbar_wait(&full[w % NB], (w / NB) & 1, kTmaWaitCycles);
 		}
 		return;
 	}
@@ -315,9 +347,12 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 #pragma unroll
 			for (int q = 0; q < G::NIN; q++)
 				if (G::staged(q)) sb[q] = s == 0 ? G::slot(q, k) : G::step_slot(q, sb[q], 1);
-			const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[gs % NB], (gs / NB) & 1));
+			const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[gs % NB], (gs / NB) & 1, wait, abort));
 			if (!ok) {
-				if ((tid & 31) == 0) atomicExch(err, 1);
+				if ((tid & 31) == 0) {
+					*abort = 1;
+					atomicExch(err, 1);
+				}
 				return;
 			}
 #pragma unroll
@@ -375,6 +410,8 @@ namespace kg {
 cudaError_t tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, const void* base, uint64_t nx,
 	uint64_t ny, uint64_t ns, int elem_bytes, int box_w, int box_h);
 int* tma_error_flag();
+// Clock cycles a compute warp waits for its copies (kg_set_tma_wait_limit).
+long long tma_wait_limit();
 
 template <class S> struct TmaType;
 template <> struct TmaType<float> { static constexpr CUtensorMapDataType v = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; };
@@ -435,24 +472,28 @@ struct TmaLaunch {
 		if (dx <= 0 || dy <= 0 || dz <= 0) return cudaSuccess;
 		constexpr int threads = kThreads;
 		constexpr size_t smem = G::total();
-		static int per_sm_of[64], sms_of[64];   // per device: resident CTAs per SM, SMs
+		// per device: resident CTAs per SM and SMs, packed in one atomic word
+		// (host threads may race to fill it; both write the same value)
+		static std::atomic<int> occ_of[64];
 		int dev = 0;
 		cudaError_t e = cudaGetDevice(&dev);
 		if (e != cudaSuccess) return e;
 		if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-		if (!per_sm_of[dev]) {
+		int occ = occ_of[dev].load(std::memory_order_acquire);
+		if (!occ) {
 			if ((e = cudaFuncSetAttribute(func(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
 				return e;
 			int b = 0, n = 0;
 			if ((e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
 			if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, tma_kernel<K, N, S, TX, TY, PY, L>, threads, smem)) != cudaSuccess)
 				return e;
-			sms_of[dev] = n;
-			per_sm_of[dev] = b > 0 ? b : 1;
+			occ = ((b > 0 ? b : 1) << 16) | (n & 0xffff);
+			occ_of[dev].store(occ, std::memory_order_release);
 		}
-		const int per_sm = per_sm_of[dev], sms = sms_of[dev];
+		const int per_sm = occ >> 16, sms = occ & 0xffff;
 		int* err = tma_error_flag();
 		if (!err) return cudaErrorInvalidSymbol;
+		const long long wait = tma_wait_limit();
 		TMaps maps;
 		memset(&maps, 0, sizeof(maps));
 		for (int q = 0; q < sl.nin; q++) {
@@ -483,7 +524,7 @@ struct TmaLaunch {
 		// y tiles beyond the grid's limit (65535) go to further launches
 		for (int y0 = 0; y0 < gy; y0 += 65535) {
 			dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
-			tma_kernel<K, N, S, TX, TY, PY, L><<<grid, threads, smem, st>>>(kop, p, maps, nx, ny, ns, kc, y0, err);
+			tma_kernel<K, N, S, TX, TY, PY, L><<<grid, threads, smem, st>>>(kop, p, maps, nx, ny, ns, kc, y0, err, wait);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
 		}
 		return cudaSuccess;

@@ -39,7 +39,7 @@ EXPORTS = [
     "kg_batch_set_config", "kg_batch_get_config", "kg_batch_set_step", "kg_batch_final_roles",
     "kg_batch_destroy", "kg_poisson_solve", "kg_engine_status",
     "kg_vecadd", "kg_matvec", "kg_matmul", "kg_sincos", "kg_whispering", "kg_extra_regcount",
-    "kg_plan_kernels", "kg_exact_arith",
+    "kg_plan_kernels", "kg_exact_arith", "kg_set_tma_wait_limit",
 ]
 EXTRA_TESTS = ["vecadd", "matvec", "matmul", "sincos", "whispering"]
 KG_ENGINE_AUTO, KG_ENGINE_DIRECT, KG_ENGINE_STAGED, KG_ENGINE_TMA = 0, 1, 2, 3
@@ -120,6 +120,7 @@ def _sig(lib):
         "kg_gameoflife": [I, I, I, P, P, P],
         "kg_sweep": [ctypes.POINTER(KgProblem), P],
         "kg_engine_status": [P],
+        "kg_set_tma_wait_limit": [ctypes.c_longlong],
         "kg_vecadd": [I, I, I, I, P, P, P, P],
         "kg_matvec": [I, I, I, P, P, P, P],
         "kg_matmul": [I, I, I, I, P, P, P, P],

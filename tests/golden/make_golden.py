@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Generate the golden fixtures of this directory from the reference itself.
 
-Needs the reference tree (REFERENCE, default /root/reference) and the builds
+Needs the reference tree (KG_REFERENCE_TREE, else the build's default) and the builds
 of its own C sources made by ``make -C oracle ref`` (oracle/_ref/).  The
 fixtures are committed; nothing at test time reads the reference tree.
 
@@ -32,7 +32,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 REF_BUILD = os.path.join(ROOT, "oracle", "_ref")
-REFERENCE = os.environ.get("REFERENCE", "/root/reference")
+sys.path.insert(0, ROOT)
+from __graft_entry__ import reference_tree  # noqa: E402
+
+REFERENCE = reference_tree()
 
 libc = ctypes.CDLL("libc.so.6")
 RAND_MAX = 2147483647

@@ -2,7 +2,7 @@
 """Golden fixtures of the suite's other C tests (vecadd, matvec, whispering)
 from the reference itself.
 
-Needs the reference tree (REFERENCE, default /root/reference) and
+Needs the reference tree (KG_REFERENCE_TREE, else the build's default) and
 ``make -C oracle ref``.  Writes reference_extra.json: for small cases, the
 SHA-256 of every array after nt steps of the reference kernel compiled
 unmodified in strict IEEE mode (driven with the reference main()'s rand()

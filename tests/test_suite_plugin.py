@@ -6,12 +6,16 @@ reports their rows as FAIL; the test checks the harness found and ran them.
 """
 import os
 import subprocess
+import sys
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SUITE = os.path.join(ROOT, "kernelgen-perf-tests_gb300", "suite")
-REFERENCE = os.environ.get("KG_REFERENCE_TREE", "/root/reference")
+sys.path.insert(0, ROOT)
+from __graft_entry__ import reference_tree  # noqa: E402
+
+REFERENCE = reference_tree()
 TESTS = ["laplacian", "divergence", "gradient", "uxx1", "wave13pt", "tricubic", "tricubic2",
          "jacobi", "lapgsrb", "gaussblur", "gameoflife"]
 
