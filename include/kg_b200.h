@@ -178,7 +178,10 @@ typedef enum {
 	KG_ENGINE_AUTO = 0,
 	KG_ENGINE_DIRECT = 1,   /* one thread per column, neighbours through L1     */
 	KG_ENGINE_STAGED = 2,   /* halo planes in shared memory, loaded by threads  */
-	KG_ENGINE_TMA = 3       /* halo planes in shared memory by tiled bulk copy  */
+	KG_ENGINE_TMA = 3,      /* halo planes in shared memory by tiled bulk copy  */
+	KG_ENGINE_TMA_VEC = 4   /* the same copies; each thread evaluates 4
+	                           consecutive points from vector reads (3D ops,
+	                           FP32 arithmetic: KG_F32, KG_BF16, KG_F16)     */
 } kg_engine;
 
 typedef struct {

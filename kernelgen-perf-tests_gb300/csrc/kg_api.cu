@@ -61,11 +61,12 @@ static const Meta k_meta[KG_NSTENCILS] = {
 // Engines built per storage type, bit e = kg_engine e (kg_dispatch.cuh).
 static int engines_built(int dt)
 {
-	const int d = 1 << KG_ENGINE_DIRECT, st = 1 << KG_ENGINE_STAGED, t = 1 << KG_ENGINE_TMA;
+	const int d = 1 << KG_ENGINE_DIRECT, st = 1 << KG_ENGINE_STAGED, t = 1 << KG_ENGINE_TMA,
+		tv = 1 << KG_ENGINE_TMA_VEC;
 	switch (dt) {
 	case KG_F64: case KG_F64_FMA: return d | t;
 	case KG_F64_FF: return st | t;
-	case KG_F32: case KG_BF16: case KG_F16: return d | t | (KG_FF_STAGED ? st : 0);
+	case KG_F32: case KG_BF16: case KG_F16: return d | t | tv | (KG_FF_STAGED ? st : 0);
 	case KG_U8: case KG_F64_MIX: return d;
 	default: return 0;
 	}
@@ -89,21 +90,23 @@ static kg_status validate(const kg_problem* p)
 	if (p->dtype == KG_U8 && p->stencil != KG_GAMEOFLIFE)
 		return fail(KG_ENOTSUP, "%s: byte cells are provided for gameoflife only", m.name);
 	if (p->nx < 0 || p->ny < 0 || p->ns < 0) return fail(KG_EINVAL, "%s: negative size", m.name);
-	if (p->engine < KG_ENGINE_AUTO || p->engine > KG_ENGINE_TMA)
+	if (p->engine < KG_ENGINE_AUTO || p->engine > KG_ENGINE_TMA_VEC)
 		return fail(KG_EINVAL, "%s: unknown engine %d", m.name, p->engine);
 	if (p->engine != KG_ENGINE_AUTO && !((engines_built(p->dtype) >> p->engine) & 1))
 		return fail(KG_ENOTSUP, "%s: engine %d is not built for dtype %d", m.name, p->engine, p->dtype);
 	if (m.is2d && p->ns != 1) return fail(KG_EINVAL, "%s: 2D stencil needs ns == 1", m.name);
+	if (p->engine == KG_ENGINE_TMA_VEC && m.is2d)
+		return fail(KG_ENOTSUP, "%s: the vector TMA engine is built for 3D stencils", m.name);
 	const size_t n = (size_t)p->nx * (size_t)p->ny * (size_t)p->ns;
 	if (n == 0) return KG_OK;
 	if (n > ((size_t)1 << 40)) return fail(KG_EINVAL, "%s: %zu points is beyond the supported size", m.name, n);
 	const size_t bytes = n * dtype_size(p->dtype);
 	for (int q = 0; q < m.narr; q++)
 		if (!p->arr[q]) return fail(KG_EINVAL, "%s: array %d is null", m.name, q);
-	if (p->engine == KG_ENGINE_TMA) {
+	if (p->engine == KG_ENGINE_TMA || p->engine == KG_ENGINE_TMA_VEC) {
 		bool aligned = ((size_t)p->nx * dtype_size(p->dtype)) % 16 == 0;
 		for (int q = 0; q < m.narr; q++) aligned = aligned && (uintptr_t)p->arr[q] % 16 == 0;
-		if (!aligned) return fail(KG_EINVAL, "%s: the TMA engine needs 16-byte aligned arrays and rows", m.name);
+		if (!aligned) return fail(KG_EINVAL, "%s: the TMA engines need 16-byte aligned arrays and rows", m.name);
 	}
 	// Outputs must not overlap any other array (a sweep reads its inputs while
 	// writing its outputs from other threads).

@@ -25,6 +25,7 @@
 #include "kg_engine.cuh"
 #include "kg_staged.cuh"
 #include "kg_tma.cuh"
+#include "kg_tmavec.cuh"
 
 namespace kg {
 
@@ -39,8 +40,17 @@ template <class N> struct Engines {
 	static constexpr bool direct = !ff2;
 	static constexpr bool staged = ff2 || (ff && KG_FF_STAGED);
 	static constexpr bool tma = true;
+	static constexpr bool tma_vec = ff;
 	static constexpr int automatic = ff2 ? KG_ENGINE_STAGED : ff ? KG_ENGINE_TMA : KG_ENGINE_DIRECT;
 };
+
+// FP32 arithmetic: the stencils that run on the vector TMA engine by default
+// (3D ops; where its arrays allow it, else the TMA or direct engine).
+inline bool tma_vec_preferred(int stencil)
+{
+	return stencil == KG_LAPLACIAN || stencil == KG_DIVERGENCE || stencil == KG_GRADIENT ||
+		stencil == KG_UXX1 || stencil == KG_LAPGSRB || stencil == KG_WAVE13PT;
+}
 
 inline bool tma_preferred(int stencil, int elem_bytes)
 {
@@ -64,6 +74,8 @@ template <class Op, class N, class S>
 int resolve_engine(const kg_problem& pr)
 {
 	if (pr.engine != KG_ENGINE_AUTO) return pr.engine;
+	if constexpr (Engines<N>::tma_vec)
+		if (tma_vec_preferred(pr.stencil) && TmaVecLaunch<Op, N, S>::usable(pr)) return KG_ENGINE_TMA_VEC;
 	const int e = automatic_engine<N, S>(pr.stencil);
 	if (e == KG_ENGINE_TMA && !TmaLaunch<Op, N, S>::usable(pr))
 		return Engines<N>::ff2 ? KG_ENGINE_STAGED : KG_ENGINE_DIRECT;
@@ -76,6 +88,9 @@ cudaError_t sweep_typed(const kg_problem& pr, cudaStream_t st)
 	return with_op<N>(pr, [&](const auto& op) -> cudaError_t {
 		using Op = std::decay_t<decltype(op)>;
 		const int e = resolve_engine<Op, N, S>(pr);
+		if constexpr (Engines<N>::tma_vec)
+			if (e == KG_ENGINE_TMA_VEC)
+				return TmaVecLaunch<Op, N, S>::usable(pr) ? TmaVecLaunch<Op, N, S>::run(op, pr, st) : cudaErrorInvalidValue;
 		if constexpr (Engines<N>::tma)
 			if (e == KG_ENGINE_TMA)
 				return TmaLaunch<Op, N, S>::usable(pr) ? TmaLaunch<Op, N, S>::run(op, pr, st) : cudaErrorInvalidValue;
@@ -94,7 +109,12 @@ cudaError_t regs_typed(const kg_problem& pr, int* nregs)
 	return with_op<N>(pr, [&](const auto& op) -> cudaError_t {
 		using Op = std::decay_t<decltype(op)>;
 		const void* f = nullptr;
-		const int e = automatic_engine<N, S>(pr.stencil);
+		int e = automatic_engine<N, S>(pr.stencil);
+		if constexpr (Engines<N>::tma_vec)
+			if (tma_vec_preferred(pr.stencil) && TmaVecLaunch<Op, N, S>::built) {
+				f = TmaVecLaunch<Op, N, S>::func();
+				e = -1;
+			}
 		if constexpr (Engines<N>::tma)
 			if (e == KG_ENGINE_TMA) f = TmaLaunch<Op, N, S>::func();
 		if constexpr (Engines<N>::staged)

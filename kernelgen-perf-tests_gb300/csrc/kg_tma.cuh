@@ -237,6 +237,51 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
+// The producer of a TMA-engine CTA (one thread): issues each step's copies
+// onto full[step % NB] once the step NB earlier is done (done[]), so up to
+// NB - 1 = L steps of copies are in flight ahead of the compute warps; each
+// run along z starts with its whole window of planes.  Waits for the compute
+// warps are bounded by kTmaWaitCycles and end early once a compute warp has
+// raised the CTA's abort flag; the thread then stops issuing and waits for
+// every copy it issued to land before it returns.  Normally it returns after
+// the compute warps are done with the last step.
+template <class Op, class S, class G>
+__device__ __forceinline__ void tma_produce(const TMaps& maps, unsigned char* sm, uint64_t* full, uint64_t* done,
+	const volatile int* abort, int xt, int yt, int kend, int kc, int* err)
+{
+	constexpr int NB = G::NB, L = G::NB - 1;
+#pragma unroll
+	for (int q = 0; q < G::NIN; q++)
+		if (G::staged(q)) tma_prefetch_map(&maps.m[q]);
+	uint32_t g = 0, issued = 0;   // steps issued so far
+	bool ok = true;
+	for (int kb = Op::LZ + blockIdx.z * kc; kb < kend && ok; kb += gridDim.z * kc) {
+		const int nsteps = min(kc, kend - kb);
+		// a new run's window may reuse any slot: wait for the previous run
+		if (g > 0) ok = mbar_wait(&done[(g - 1) % NB], ((g - 1) / NB) & 1, kTmaWaitCycles, abort);
+		for (int t = 0; t < nsteps && ok; t++) {
+			const uint32_t gt = g + t;
+			if (t >= L + 1) ok = mbar_wait(&done[(gt - L - 1) % NB], ((gt - L - 1) / NB) & 1, kTmaWaitCycles, abort);
+			if (!ok) break;
+			fence_proxy_async();
+			tma_issue<Op, S, G>(maps, sm, &full[gt % NB], xt, yt, kb + t, t == 0);
+			issued = gt + 1;
+		}
+		g += nsteps;
+	}
+	// stay until the compute warps are done with the last step, or gave up
+	if (ok && issued > 0) ok = mbar_wait(&done[(issued - 1) % NB], ((issued - 1) / NB) & 1, kTmaWaitCycles, abort);
+	if (!ok) {
+		atomicExch(err, 1);
+		// Every step before the last NB issued is done (the copies of step
+		// w + NB were issued only after step w was done): the copies still
+		// in flight belong to those NB steps, and they land before the
+		// CTA's shared memory goes away.
+		for (uint32_t w = issued > NB ? issued - NB : 0; w < issued; w++)
+			mbar_wait(&full[w % NB], (w / NB) & 1, kTmaWaitCycles);
+	}
+}
+
 // TX*TY compute threads and one producer warp.  Step t of a run (plane kb+t)
 // has two mbarriers: full[t % NB] completes when the step's copies have
 // landed, done[t % NB] when every compute warp has evaluated the step.  The
@@ -278,38 +323,7 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 	__syncthreads();
 
 	if (tid >= NC) {
-		// ---- producer warp (one thread) ----
-		if (tid != NC) return;
-#pragma unroll
-		for (int q = 0; q < G::NIN; q++)
-			if (G::staged(q)) tma_prefetch_map(&maps.m[q]);
-		uint32_t g = 0, issued = 0;   // steps issued so far
-		bool ok = true;
-		for (int kb = Op::LZ + blockIdx.z * kc; kb < kend && ok; kb += gridDim.z * kc) {
-			const int nsteps = min(kc, kend - kb);
-			// a new run's window may reuse any slot: wait for the previous run
-			if (g > 0) ok = mbar_wait(&done[(g - 1) % NB], ((g - 1) / NB) & 1, kTmaWaitCycles, abort);
-			for (int t = 0; t < nsteps && ok; t++) {
-				const uint32_t gt = g + t;
-				if (t >= L + 1) ok = mbar_wait(&done[(gt - L - 1) % NB], ((gt - L - 1) / NB) & 1, kTmaWaitCycles, abort);
-				if (!ok) break;
-				fence_proxy_async();
-				tma_issue<Op, S, G>(maps, sm, &full[gt % NB], xt, yt, kb + t, t == 0);
-				issued = gt + 1;
-			}
-			g += nsteps;
-		}
-		// stay until the compute warps are done with the last step, or gave up
-		if (ok && issued > 0) ok = mbar_wait(&done[(issued - 1) % NB], ((issued - 1) / NB) & 1, kTmaWaitCycles, abort);
-		if (!ok) {
-			atomicExch(err, 1);
-			// Every step before the last NB issued is done (the copies of step
-			// w + NB were issued only after step w was done): the copies still
-			// in flight belong to those NB steps, and they land before the
-			// CTA's shared memory goes away.
-			for (uint32_t w = issued > NB ? issued - NB : 0; w < issued; w++)
-				mbar_wait(&full[w % NB], (w / NB) & 1, kTmaWaitCycles);
-		}
+		if (tid == NC) tma_produce<Op, S, G>(maps, sm, full, done, abort, xt, yt, kend, kc, err);
 		return;
 	}
 
@@ -413,6 +427,23 @@ int* tma_error_flag();
 // Clock cycles a compute warp waits for its copies (kg_set_tma_wait_limit).
 long long tma_wait_limit();
 
+// Planes per run along z: z is split into runs so that the CTAs fill whole
+// waves of per_sm x sms, weighing each run's extra window planes.
+inline int tma_run_length(int per_sm, int sms, long long tiles, int dz, int nzmax)
+{
+	const long long slots = (long long)per_sm * sms;
+	int nz = 1;
+	double best = 1e300;
+	for (int c = 1; c <= min(dz, 256); c++) {
+		const long long ctas = tiles * c;
+		const double waves = (double)((ctas + slots - 1) / slots);
+		const int run = (dz + c - 1) / c;
+		const double cost = waves * (run + nzmax - 1 + 2);
+		if (cost < best * 0.999) { best = cost; nz = c; }
+	}
+	return (dz + nz - 1) / nz;
+}
+
 template <class S> struct TmaType;
 template <> struct TmaType<float> { static constexpr CUtensorMapDataType v = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; };
 template <> struct TmaType<double> { static constexpr CUtensorMapDataType v = CU_TENSOR_MAP_DATA_TYPE_FLOAT64; };
@@ -504,20 +535,8 @@ struct TmaLaunch {
 		}
 		const int gx = (nx - K::HX + TX - 1) / TX;
 		const int gy = (dy + TY * PY - 1) / (TY * PY);
-		// Split z into runs so that the CTAs fill whole waves, weighing each
-		// run's extra window planes.
-		const long long slots = (long long)per_sm * sms, tiles = (long long)gx * gy;
-		int nz = 1;
-		double best = 1e300;
-		for (int c = 1; c <= min(dz, 256); c++) {
-			const long long ctas = tiles * c;
-			const double waves = (double)((ctas + slots - 1) / slots);
-			const int run = (dz + c - 1) / c;
-			const double cost = waves * (run + G::NZMAX() - 1 + 2);
-			if (cost < best * 0.999) { best = cost; nz = c; }
-		}
-		const int kc = (dz + nz - 1) / nz;
-		nz = (dz + kc - 1) / kc;
+		const int kc = tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX());
+		const int nz = (dz + kc - 1) / kc;
 		K kop;
 		if constexpr (k2d) kop.op = op;
 		else kop = op;

@@ -1,0 +1,272 @@
+// kg_tmavec.cuh -- the TMA engine with V consecutive points per thread.
+//
+// The copies, rings, mbarriers and the producer are those of the TMA engine
+// (kg_tma.cuh); only the compute side differs.  A compute warp owns one row
+// of the CTA's tile, 32 * V consecutive columns, and each lane evaluates V
+// consecutive points of it, so every neighbour row the body reads is fetched
+// from shared memory as whole vectors: the V values of the lane's own
+// columns (one 16-byte load for V = 4 FP32 values) and, where the body reaches
+// left or right of them, the V values before or after.  The body itself is
+// evaluated V times with its accessor shifted by one column each time; the
+// compiler merges the identical vector loads of the V evaluations, so a
+// 7-point body costs about 7 vector loads per V points instead of 7 scalar
+// loads per point, and the outputs leave as one vector store per row.
+//
+// For 3D ops with storage of 4 or 2 bytes (FP32, BF16, FP16; FP32
+// arithmetic) whose reach along x is at most V on either side.
+#pragma once
+
+#include "kg_tma.cuh"
+
+namespace kg {
+
+template <class S, int V> struct alignas(V * sizeof(S)) VPack {
+	S v[V];
+};
+
+// Element x (0 <= x < 3V) of the 3V stored values that start V columns left
+// of the lane's first column, row_elems elements after the lane's base.
+template <class S, int V>
+__device__ __forceinline__ S vrow_load(const unsigned char* b, int row_elems, int x)
+{
+	const int chunk = x / V - 1;   // -1, 0, 1
+	const VPack<S, V> pk = *reinterpret_cast<const VPack<S, V>*>(b + (row_elems + chunk * V) * (int)sizeof(S));
+	return pk.v[x % V];
+}
+
+template <class Op, class N, class S, class G, int V, int VI> struct VAcc {
+	static constexpr int ZS = 5;
+	const unsigned char* (*base)[ZS];   // per input and dz + z0: the lane's first column in the point's row
+	const S* const* in;
+	long long c, sy, sz;                      // c: the lane's first point
+	__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
+		return Conv<N, S>::from(vrow_load<S, V>(base[q][dz + Op::halo(q).z0], dy * G::W(q), VI + dx + V));
+	}
+	__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
+		return __ldg(in[q] + c + VI + dx + dy * sy + dz * sz);
+	}
+};
+
+// V outputs of one lane to global memory: one vector store where all V
+// points are in the domain, else one store per point that is.
+template <class S, int V>
+__device__ __forceinline__ void vstore(S* dst, const S (&o)[V], unsigned valid_mask)
+{
+	if (valid_mask == (1u << V) - 1) {
+		VPack<S, V> pk;
+#pragma unroll
+		for (int v = 0; v < V; v++) pk.v[v] = o[v];
+		*reinterpret_cast<VPack<S, V>*>(dst) = pk;
+	} else {
+#pragma unroll
+		for (int v = 0; v < V; v++)
+			if ((valid_mask >> v) & 1u) dst[v] = o[v];
+	}
+}
+
+template <int I, int V, class F> __device__ __forceinline__ void for_v(F&& f)
+{
+	if constexpr (I < V) {
+		f(std::integral_constant<int, I>{});
+		for_v<I + 1, V>(f);
+	}
+}
+
+// NW compute warps (one row of the tile each) and one producer warp; the
+// tile is 32 V columns x NW rows of every plane of a run along z.
+template <class Op, class N, class S, int V, int NW, int L>
+__global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p, const __grid_constant__ TMaps maps,
+	int nx, int ny, int ns, int kc, int yt0, int* err, long long wait)
+{
+	constexpr int BX = 32 * V, BY = NW, NC = 32 * NW;
+	using G = TGeo<Op, S, BX, BY, L>;
+	constexpr int NB = G::NB;
+	constexpr Slots sl = Op::slots();
+	constexpr int ZS = VAcc<Op, N, S, G, V, 0>::ZS;
+	static_assert(G::fits(), "tile does not fit the TMA engine");
+	static_assert(G::NZMAX() <= ZS, "at most ZS planes per window");
+	extern __shared__ __align__(128) unsigned char sm[];
+	uint64_t* full = reinterpret_cast<uint64_t*>(sm);
+	uint64_t* done = full + NB;
+	volatile int* abort = reinterpret_cast<volatile int*>(sm + G::kAbort);
+
+	const int tid = threadIdx.x;
+	const int xt = blockIdx.x * BX, yt = Op::LY + (yt0 + (int)blockIdx.y) * BY;
+	const int kend = ns - Op::HZ;
+
+	if (tid == 0) {
+		for (int b = 0; b < NB; b++) {
+			mbar_init(&full[b], 1);
+			mbar_init(&done[b], NW);
+		}
+		*abort = 0;
+		mbar_fence_init();
+	}
+	__syncthreads();
+
+	if (tid >= NC) {
+		if (tid == NC) tma_produce<Op, S, G>(maps, sm, full, done, abort, xt, yt, kend, kc, err);
+		return;
+	}
+
+	// ---- compute warps ----
+	const int lane = tid & 31, w = tid >> 5;
+	const int i0 = xt + lane * V, j = yt + w;
+	const long long sy = nx, sz = (long long)nx * ny;
+	const bool row_ok = j < ny - Op::HY;
+	unsigned valid = 0;
+#pragma unroll
+	for (int v = 0; v < V; v++)
+		if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid |= 1u << v;
+	// byte offset of the lane's first column in the point's row of a plane, per input
+	int toff[6];
+#pragma unroll
+	for (int q = 0; q < G::NIN; q++)
+		toff[q] = ((w + Op::halo(q).y0) * G::W(q) + lane * V + G::XL(q)) * G::ES;
+
+	uint32_t g = 0;
+	for (int kb = Op::LZ + blockIdx.z * kc; kb < kend; kb += gridDim.z * kc) {
+		const int nsteps = min(kc, kend - kb);
+		for (int s = 0; s < nsteps; s++) {
+			const int k = kb + s;
+			const uint32_t gs = g + s;
+			const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[gs % NB], (gs / NB) & 1, wait, abort));
+			if (!ok) {
+				if (lane == 0) {
+					*abort = 1;
+					atomicExch(err, 1);
+				}
+				return;
+			}
+			const unsigned char* base[6][ZS];
+#pragma unroll
+			for (int q = 0; q < G::NIN; q++) {
+				const Halo h = Op::halo(q);
+				const int s0 = G::slot(q, k);
+#pragma unroll
+				for (int d = 0; d < ZS; d++)
+					if (d < G::NZ(q))
+						base[q][d] = sm + G::offset(q) + G::step_slot(q, s0, d - h.z0) * G::PS(q) + toff[q];
+			}
+			const long long c = i0 + sy * j + sz * k;
+			S o[3][V];
+			for_v<0, V>([&](auto vi) {
+				constexpr int VI = decltype(vi)::value;
+				VAcc<Op, N, S, G, V, VI> at{base, p.in, c, sy, sz};
+				N r[3];
+				op.point(at, r);
+#pragma unroll
+				for (int q = 0; q < sl.nout; q++) o[q][VI] = Conv<N, S>::to(r[q]);
+			});
+			// this warp is done with the step's planes
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&done[gs % NB]);
+			if (valid) {
+#pragma unroll
+				for (int q = 0; q < sl.nout; q++) vstore<S, V>(p.out[q] + c, o[q], valid);
+			}
+		}
+		g += nsteps;
+	}
+}
+
+// Shared memory per CTA for the rings: L (steps of copies in flight) is the
+// largest, up to 6, whose rings fit this budget; the CTAs per SM follow from
+// what the rings then take.
+#ifndef KG_TMAVEC_BUDGET
+#define KG_TMAVEC_BUDGET (100 * 1024)
+#endif
+template <class Op, class S, int BX, int BY> struct TmaVecDepth {
+	template <int L> static constexpr int bytes() { return TGeo<Op, S, BX, BY, L>::total(); }
+	static constexpr int kBudget = KG_TMAVEC_BUDGET;
+	static constexpr int L = bytes<6>() <= kBudget ? 6 : bytes<5>() <= kBudget ? 5 : bytes<4>() <= kBudget ? 4
+		: bytes<3>() <= kBudget ? 3 : bytes<2>() <= kBudget ? 2 : 1;
+};
+
+template <class Op, class N, class S>
+struct TmaVecLaunch {
+	static constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
+	static constexpr int V = 4, NW = 8;
+	static constexpr int BX = 32 * V, BY = NW;
+	static constexpr int L = TmaVecDepth<Op, S, BX, BY>::L;
+	static constexpr int kThreads = 32 * NW + 32;
+	using G = TGeo<Op, S, BX, BY, L>;
+	static constexpr bool reach_ok() {
+		for (int q = 0; q < Op::slots().nin; q++)
+			if (Op::halo(q).x0 > V || Op::halo(q).x1 > V) return false;
+		return true;
+	}
+	// built for 3D ops on 4- and 2-byte storage whose reach along x fits
+	static constexpr bool built = !k2d && sizeof(S) <= 4 && reach_ok();
+	static const void* func() {
+		if constexpr (built) return (const void*)tma_vec_kernel<Op, N, S, V, NW, L>;
+		else return nullptr;
+	}
+
+	// The copies need 16-byte aligned input arrays and rows; the vector
+	// stores need V-element aligned outputs.
+	static bool usable(const kg_problem& pr) {
+		if constexpr (!built) return false;
+		constexpr Slots sl = Op::slots();
+		if (((size_t)pr.nx * sizeof(S)) % 16) return false;
+		for (int q = 0; q < sl.nin; q++)
+			if ((uintptr_t)pr.arr[sl.in[q]] % 16) return false;
+		for (int q = 0; q < sl.nout; q++)
+			if ((uintptr_t)pr.arr[sl.out[q]] % (V * sizeof(S))) return false;
+		return true;
+	}
+
+	static cudaError_t run(const Op& op, const kg_problem& pr, cudaStream_t st) {
+		if constexpr (!built) {
+			return cudaErrorNotSupported;
+		} else {
+			constexpr Slots sl = Op::slots();
+			Ptrs<S> p{};
+			for (int q = 0; q < sl.nin; q++) p.in[q] = (const S*)pr.arr[sl.in[q]];
+			for (int q = 0; q < sl.nout; q++) p.out[q] = (S*)pr.arr[sl.out[q]];
+			const int nx = pr.nx, ny = pr.ny, ns = pr.ns;
+			const int dx = nx - Op::LX - Op::HX, dy = ny - Op::LY - Op::HY, dz = ns - Op::LZ - Op::HZ;
+			if (dx <= 0 || dy <= 0 || dz <= 0) return cudaSuccess;
+			constexpr size_t smem = G::total();
+			static std::atomic<int> occ_of[64];
+			int dev = 0;
+			cudaError_t e = cudaGetDevice(&dev);
+			if (e != cudaSuccess) return e;
+			if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+			int occ = occ_of[dev].load(std::memory_order_acquire);
+			if (!occ) {
+				if ((e = cudaFuncSetAttribute(func(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+					return e;
+				int b = 0, n = 0;
+				if ((e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+				if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, tma_vec_kernel<Op, N, S, V, NW, L>, kThreads, smem)) != cudaSuccess)
+					return e;
+				occ = ((b > 0 ? b : 1) << 16) | (n & 0xffff);
+				occ_of[dev].store(occ, std::memory_order_release);
+			}
+			const int per_sm = occ >> 16, sms = occ & 0xffff;
+			int* err = tma_error_flag();
+			if (!err) return cudaErrorInvalidSymbol;
+			const long long wait = tma_wait_limit();
+			TMaps maps;
+			memset(&maps, 0, sizeof(maps));
+			for (int q = 0; q < sl.nin; q++) {
+				if (!G::staged(q)) continue;
+				e = tma_encode_3d(&maps.m[q], TmaType<S>::v, p.in[q], nx, ny, ns, (int)sizeof(S), G::W(q), G::H(q));
+				if (e != cudaSuccess) return e;
+			}
+			const int gx = (nx - Op::HX + BX - 1) / BX;
+			const int gy = (dy + BY - 1) / BY;
+			const int kc = tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX());
+			const int nz = (dz + kc - 1) / kc;
+			for (int y0 = 0; y0 < gy; y0 += 65535) {
+				dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
+				tma_vec_kernel<Op, N, S, V, NW, L><<<grid, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, kc, y0, err, wait);
+				if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			}
+			return cudaSuccess;
+		}
+	}
+};
+
+}  // namespace kg

@@ -14,7 +14,7 @@
  *   B200_INIT  reference (default) | bernoulli | unit | pulse
  *   B200_MODE  plain (default: one launch per sweep, timed) | graph (the
  *              nt-sweep loop replayed as one CUDA graph)
- *   B200_ENGINE auto (default) | direct | staged | tma (kg_problem.engine)
+ *   B200_ENGINE auto (default) | direct | staged | tma | tmavec (kg_problem.engine)
  *   NO_TIMING, PROFILING_FNAME as in the reference.
  * With PROFILING_FNAME set it prints "<name> regcount = N" and, per sweep,
  * "<name> kernel time = t", the two lines the reference's launch interposer
@@ -86,6 +86,7 @@ static int parse_engine(const char* s)
 	if (!strcmp(s, "direct")) return KG_ENGINE_DIRECT;
 	if (!strcmp(s, "staged")) return KG_ENGINE_STAGED;
 	if (!strcmp(s, "tma")) return KG_ENGINE_TMA;
+	if (!strcmp(s, "tmavec")) return KG_ENGINE_TMA_VEC;
 	fprintf(stderr, "Unknown B200_ENGINE=%s\n", s);
 	exit(1);
 }

@@ -42,9 +42,10 @@ EXPORTS = [
     "kg_plan_kernels", "kg_exact_arith", "kg_set_tma_wait_limit",
 ]
 EXTRA_TESTS = ["vecadd", "matvec", "matmul", "sincos", "whispering"]
-KG_ENGINE_AUTO, KG_ENGINE_DIRECT, KG_ENGINE_STAGED, KG_ENGINE_TMA = 0, 1, 2, 3
+KG_ENGINE_AUTO, KG_ENGINE_DIRECT, KG_ENGINE_STAGED, KG_ENGINE_TMA, KG_ENGINE_TMA_VEC = 0, 1, 2, 3, 4
 KG_ARITH_ADD, KG_ARITH_MUL, KG_ARITH_DIV, KG_ARITH_NATIVE_ADD, KG_ARITH_NATIVE_MUL, KG_ARITH_NATIVE_DIV = range(6)
-ENGINES = {"auto": KG_ENGINE_AUTO, "direct": KG_ENGINE_DIRECT, "staged": KG_ENGINE_STAGED, "tma": KG_ENGINE_TMA}
+ENGINES = {"auto": KG_ENGINE_AUTO, "direct": KG_ENGINE_DIRECT, "staged": KG_ENGINE_STAGED, "tma": KG_ENGINE_TMA,
+           "tmavec": KG_ENGINE_TMA_VEC}
 KG_SOLVE_SOR_F64, KG_SOLVE_IR_SOR_F32, KG_SOLVE_IR_JACOBI_F32 = 0, 1, 2
 
 
