@@ -566,12 +566,26 @@ def run_batched(nsteps=50, reps=3, tune_cache=None):
     b32.tune(tune_cache, stream)
     out["tune_s"] = round(time.perf_counter() - t0, 3)
     cfg = b32.config()
-    out["tuned"] = {"bx": cfg.bx, "by": cfg.by, "kc": cfg.kc, "ctas_per_sm": cfg.ctas_per_sm, "tiles": cfg.tiles}
+    out["tuned"] = {"config": cfg.shape, "bx": cfg.bx, "by": cfg.by, "kc": cfg.kc, "temporal": cfg.temporal,
+                    "ctas_per_sm": cfg.ctas_per_sm, "tiles": cfg.tiles, "configs_tried": cfg.nshapes,
+                    "what": "temporal == 1: tiles of bx*by threads on consecutive columns, kc planes each; "
+                            "temporal T > 1: output blocks of bx x by x kc points evaluated T steps deep in "
+                            "shared memory per launch"}
     restore()
     b32.set_step(0)
     b32.capture(nsteps)
     ms = timed(lambda: b32.launch(stream))
     out["fp32_batched_graph_gpts"] = round(nsteps * npts / (ms * 1e-3) / 1e9, 2)
+    # compulsory FP32 bytes of one step (each problem's arrays once, per its stencil)
+    bpp32 = {"laplacian": 8, "divergence": 16, "wave13pt": 12, "gaussblur": 8}
+    step_bytes = sum(bpp32[nm] * int(np_prod(sh)) for nm, sh, _ in specs)
+    hbm, _ = peaks()
+    out["fp32_batched_graph_hbm"] = {
+        "algorithmic_bytes_per_step": step_bytes,
+        "gbs": round(step_bytes * nsteps / (ms * 1e-3) / 1e9, 1),
+        "frac_of_measured": round(step_bytes * nsteps / (ms * 1e-3) / 1e9 / hbm, 3),
+        "note": "algorithmic bytes of the steps over their time; with temporal blocking each value crosses "
+                "HBM about twice per T steps, so this can exceed the DRAM throughput"}
     ms = timed(lambda: b32.step(nsteps, stream))
     out["fp32_batched_launches_gpts"] = round(nsteps * npts / (ms * 1e-3) / 1e9, 2)
 

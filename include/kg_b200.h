@@ -312,18 +312,25 @@ kg_status kg_plan_destroy(kg_plan plan);
 
 /* Up to 4096 independent problems of laplacian, divergence, wave13pt and
  * gaussblur (2D, ns = 1), all KG_F32 or all KG_F64, advanced together.  Each
- * step is one persistent kernel launch over the tiles of every problem; each
- * problem's arrays rotate their roles per step as the reference loops do.
- * Results equal nsteps kg_sweep calls per problem, bit for bit.
+ * launch is one persistent kernel over the tiles of every problem and
+ * advances every problem 1 step, or T steps with temporal blocking (blocks
+ * evaluated T steps deep in shared memory; the library then keeps a second
+ * set of the rotating arrays, allocated when such a configuration is first
+ * set, and every kg_batch_step / graph replay ends with all arrays in the
+ * problems' own buffers).  Each problem's arrays rotate their roles per step
+ * as the reference loops do.  Results equal nsteps kg_sweep calls per
+ * problem, bit for bit, every array.
  * No counterpart in the reference (each suite program runs one problem). */
 typedef struct kg_batch_s* kg_batch;
 typedef struct {
-	int shape, bx, by, kc;   /* tile: BX*BY threads on as many consecutive (i,j)
-	                            columns, KC planes each (2D: KC runs of points) */
+	int shape, bx, by, kc;   /* temporal == 1: tile of BX*BY threads on as many
+	                            consecutive (i,j) columns, KC planes each (2D:
+	                            KC runs of points); temporal > 1: output block
+	                            of BX x BY x KC points (2D: BX x BY*KC)     */
 	int ctas_per_sm;
-	int tiles;               /* tiles of all problems per step */
-	int nshapes;             /* tile shapes the tuner tries */
-	int reserved;
+	int tiles;               /* tiles (blocks) of all problems per launch */
+	int nshapes;             /* configurations the tuner tries */
+	int temporal;            /* steps per launch (temporal-blocking factor) */
 	long long steps_done;
 } kg_batch_config;
 kg_status kg_batch_create(kg_batch* b, const kg_problem* probs, int nprob);
@@ -333,8 +340,10 @@ kg_status kg_batch_step(kg_batch b, int nsteps, kg_stream_t stream);
  * kg_batch_launch replays it and continues from the current step. */
 kg_status kg_batch_capture(kg_batch b, int nsteps);
 kg_status kg_batch_launch(kg_batch b, kg_stream_t stream);
-/* Times every tile shape with as many CTAs per SM as stay resident, one
- * fewer and half as many, on this batch (advancing it), and keeps the fastest; cache_path (may be NULL) stores and reuses the choice
+/* Times every configuration -- the one-step tile shapes and the temporal
+ * blocks with their factors T = 2, 3, 4 -- with as many CTAs per SM as stay
+ * resident, one fewer and half as many, on this batch (advancing it), and
+ * keeps the fastest; cache_path (may be NULL) stores and reuses the choice
  * per device and problem list. */
 kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream);
 kg_status kg_batch_set_config(kg_batch b, int shape, int ctas_per_sm);

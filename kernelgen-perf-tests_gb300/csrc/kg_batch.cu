@@ -17,9 +17,23 @@
 // the sequence advances the base, so a captured N-step graph can be replayed
 // and continue where it stopped.
 //
-// Tuning.  The tile shape (BX x BY x KC) and the CTAs per SM are chosen by
-// timing every candidate on the batch itself (kg_batch_tune); the choice is
-// cached in a text file keyed by the device and a hash of the problem list.
+// Temporal tiles.  With a temporal factor T > 1 one launch advances every
+// problem T steps: a CTA loads a block of the step's input expanded by T
+// stencil radii into shared memory (with the rims of the other time levels
+// where the block touches the domain's edge), evaluates the T steps there on
+// regions that shrink by one radius per step (the halo points are evaluated
+// redundantly by the neighbouring blocks), and writes the block of the time
+// levels the next launch reads; so a value crosses HBM about twice per T
+// steps instead of twice per step.  Each point is evaluated by the same body
+// as the single-problem sweeps, so the results are those of T sweeps, bit for
+// bit.  divergence (whose inputs never change) is evaluated T times from
+// global memory.
+//
+// Tuning.  The tile shape (BX x BY x KC, or an output block and T) and the
+// CTAs per SM are chosen by timing every candidate on the batch itself
+// (kg_batch_tune); the choice is cached in a text file keyed by the device
+// and a hash of the problem list.
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -43,6 +57,7 @@ struct BatchDesc {
 	int tiles_x, tiles_y, tiles_z, first;
 	double c[8];          // coefficients in the compute type's precision (as double)
 	void* a[4];           // arrays in their original roles
+	void* b[4];           // temporal tiles: a second set of the rotating arrays
 };
 
 // Roles of the arrays of problem d at time step `step`.
@@ -164,16 +179,315 @@ __global__ void __launch_bounds__(BX * BY, 2048 / (BX * BY)) batch_kernel(const 
 	}
 }
 
+// ---- temporal tiles ----------------------------------------------------------
+//
+// A launch of T steps reads the time levels from one set of arrays and writes
+// them to the other (the problem's own arrays a[] or its second set b[]):
+// blocks of other CTAs still read the levels a block has advanced, so the
+// levels cannot be written in place.  The host orders the launches of a
+// sequence so that the last one writes the problem's own arrays, and copies
+// the rims of the rotating arrays into the second set first (the sweeps never
+// write rims, and a level is read at its rims by the blocks at the domain's
+// edge).
+
+constexpr int kTBThreads = 256;
+
+// Bytes of the first-tile table at the start of the temporal kernel's
+// dynamic shared memory (16-byte multiple).
+__host__ __device__ __forceinline__ int tb_first_bytes(int nprob) { return ((nprob + 1) * 4 + 15) / 16 * 16; }
+
+// Output block (bx x by x bz points; 2D problems: bx x (by bz) rows) and the
+// steps per launch.
+struct TBShape { int bx, by, bz, t; };
+
+__device__ __forceinline__ void cp_async_elem(void* dst_smem, const void* src, int bytes)
+{
+	const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+	if (bytes == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+	else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+	asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// A box [x0, x0+ex) x [y0, y0+ey) x [z0, z0+ez) of array coordinates.
+struct TBBox {
+	int x0, y0, z0, ex, ey, ez;
+	__device__ __forceinline__ int n() const { return ex * ey * ez; }
+};
+
+// b grown by (rx, ry, rz) on every side, clipped to [lx, hx) x [ly, hy) x [lz, hz).
+__device__ __forceinline__ TBBox tb_grow(const TBBox& b, int rx, int ry, int rz, int lx, int ly, int lz, int hx,
+	int hy, int hz)
+{
+	TBBox o;
+	o.x0 = max(lx, b.x0 - rx);
+	o.y0 = max(ly, b.y0 - ry);
+	o.z0 = max(lz, b.z0 - rz);
+	o.ex = min(hx, b.x0 + b.ex + rx) - o.x0;
+	o.ey = min(hy, b.y0 + b.ey + ry) - o.y0;
+	o.ez = min(hz, b.z0 + b.ez + rz) - o.z0;
+	return o;
+}
+
+// Reads of a body evaluated on shared-memory time levels: input q is level
+// lev[q], element c of the region is the point, (sy, sz) the region strides.
+template <class N, class S> struct TBAcc {
+	const S* lev[2];
+	int c, sy, sz;
+	__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
+		return Conv<N, S>::from(lev[q][c + dx + dy * sy + dz * sz]);
+	}
+	__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const { return lev[q][c + dx + dy * sy + dz * sz]; }
+};
+
+// Stores of the box `b` of a level (region R in shared memory) to the global array dst.
+template <class S>
+__device__ __forceinline__ void tb_store(S* dst, const S* src, const TBBox& R, const TBBox& b, int nx, int ny)
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	for (int row = warp; row < b.ey * b.ez; row += kTBThreads / 32) {
+		const int z = row / b.ey, y = row - z * b.ey;
+		const int gy = b.y0 + y, gz = b.z0 + z;
+		const S* s = src + ((gz - R.z0) * R.ey + (gy - R.y0)) * R.ex + (b.x0 - R.x0);
+		S* d = dst + b.x0 + (long long)nx * (gy + (long long)ny * gz);
+		for (int x = lane; x < b.ex; x += 32) d[x] = s[x];
+	}
+}
+
+// Shared memory (elements of S) the blocks of a shape need for problems of
+// a stencil: NLEV levels of the output block grown by T radii.
+inline long long tb_smem_elems(int stencil, const TBShape& sh, int T)
+{
+	const bool k2d = stencil == KG_GAUSSBLUR;
+	const int r = stencil == KG_LAPLACIAN ? 1 : 2;
+	const int nlev = stencil == KG_WAVE13PT ? 3 : 2;
+	if (stencil == KG_DIVERGENCE) return 0;
+	const long long ex = sh.bx + 2 * r * T;
+	const long long ey = (k2d ? sh.by * sh.bz : sh.by) + 2 * r * T;
+	const long long ez = k2d ? 1 : sh.bz + 2 * r * T;
+	return nlev * ex * ey * ez;
+}
+
+// T steps of one output block of a problem of Op with NLEV rotating time
+// levels (2: the two-buffer swap; 3: wave13pt's levels).  Level i of the
+// shared memory mirrors array (g + i) % NLEV of the set read (rd) over the
+// region R (the block grown by T radii, clipped to the array); the levels the
+// first step reads are loaded whole, the others only where R leaves the
+// update domain (their rims).  Step s evaluates the block grown by T-1-s
+// radii (clipped to the domain) from level s and writes level s + NLEV - 1.
+// Then the block of every level the next launch reads goes to the set
+// written (wr); with all_levels, every level (the arrays as the reference
+// loop leaves them after the steps).
+template <class Op, class N, class S, int NLEV>
+__device__ void tb_block(const Op& op, const BatchDesc& d, void* const* rd, void* const* wr, long long g, int tile,
+	int T, const TBShape& sh, S* sm, bool all_levels)
+{
+	constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
+	constexpr int r = Op::LX;   // the batch's ops reach r = LX = HX = LY = HY (= LZ = HZ) points
+	const int nx = d.nx, ny = d.ny, ns = d.ns;
+	const int DX0 = Op::LX, DX1 = nx - Op::HX, DY0 = Op::LY, DY1 = ny - Op::HY;
+	const int DZ0 = Op::LZ, DZ1 = ns - Op::HZ;
+	const int bz = k2d ? 1 : sh.bz, by = k2d ? sh.by * sh.bz : sh.by;
+	const int tx = (DX1 - DX0 + sh.bx - 1) / sh.bx, ty = (DY1 - DY0 + by - 1) / by;
+	const int ix = tile % tx, iy = (tile / tx) % ty, iz = tile / (tx * ty);
+	TBBox O;
+	O.x0 = DX0 + ix * sh.bx;
+	O.y0 = DY0 + iy * by;
+	O.z0 = DZ0 + iz * bz;
+	O.ex = min(sh.bx, DX1 - O.x0);
+	O.ey = min(by, DY1 - O.y0);
+	O.ez = min(bz, DZ1 - O.z0);
+	const int rz = k2d ? 0 : r;
+	const TBBox R = tb_grow(O, r * T, r * T, rz * T, 0, 0, 0, nx, ny, ns);
+	const int RN = R.n();
+	const bool inside = R.x0 >= DX0 && R.x0 + R.ex <= DX1 && R.y0 >= DY0 && R.y0 + R.ey <= DY1 &&
+		R.z0 >= DZ0 && R.z0 + R.ez <= DZ1;
+	constexpr int nin0 = NLEV - 1;   // levels the first step reads
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll 1
+	for (int l = 0; l < NLEV; l++) {
+		if (l >= nin0 && inside) continue;
+		const S* src = (const S*)rd[(int)((g + l) % NLEV)];
+		S* lev = sm + l * RN;
+		for (int row = warp; row < R.ey * R.ez; row += kTBThreads / 32) {
+			const int z = row / R.ey, y = row - z * R.ey;
+			const int gy = R.y0 + y, gz = R.z0 + z;
+			const bool row_rim = gy < DY0 || gy >= DY1 || gz < DZ0 || gz >= DZ1;
+			const S* srow = src + (long long)nx * (gy + (long long)ny * gz);
+			for (int x = lane; x < R.ex; x += 32) {
+				const int gx = R.x0 + x;
+				if (l < nin0 || row_rim || gx < DX0 || gx >= DX1)
+					cp_async_elem(lev + row * R.ex + x, srow + gx, (int)sizeof(S));
+			}
+		}
+	}
+	cp_async_wait_all();
+	__syncthreads();
+	const int sy = R.ex, szr = R.ex * R.ey;
+	for (int st = 0; st < T; st++) {
+		const int grow = T - 1 - st;
+		const TBBox E = tb_grow(O, r * grow, r * grow, rz * grow, DX0, DY0, DZ0, DX1, DY1, DZ1);
+		const S* in0 = sm + (st % NLEV) * RN;
+		const S* in1 = sm + ((st + 1) % NLEV) * RN;
+		S* out = sm + ((st + NLEV - 1) % NLEV) * RN;
+		const int pe = E.ex * E.ey;
+		const float inv_ex = 1.0f / (float)E.ex;
+		for (int z = 0; z < E.ez; z++) {
+			const int cz = (E.z0 - R.z0 + z) * szr + (E.y0 - R.y0) * sy + (E.x0 - R.x0);
+			for (int p = threadIdx.x; p < pe; p += kTBThreads) {
+				// p / E.ex through FP32: p + 1/2 lies at least 1 / (2 E.ex) from
+				// a multiple of E.ex, far beyond FP32's rounding at these sizes
+				const int y = __float2int_rz(((float)p + 0.5f) * inv_ex);
+				const int x = p - y * E.ex;
+				const int c = cz + y * sy + x;
+				TBAcc<N, S> at{{in0, in1}, c, sy, szr};
+				N o[3];
+				op.point(at, o);
+				out[c] = Conv<N, S>::to(o[0]);
+			}
+		}
+		__syncthreads();
+	}
+	// level l holds array (g + l) % NLEV after the steps; the next launch
+	// reads levels T .. T + nin0 - 1 (mod NLEV)
+	const int nw = all_levels ? NLEV : nin0;
+#pragma unroll 1
+	for (int b = 0; b < nw; b++) {
+		const int l = (T + b) % NLEV;
+		tb_store<S>((S*)wr[(int)((g + l) % NLEV)], sm + l * RN, R, O, nx, ny);
+	}
+	__syncthreads();
+}
+
+// divergence: T evaluations of the block from global memory (its inputs
+// never change, so each step writes the same values to the same array).
+template <class N, class S>
+__device__ void tb_divergence(const BatchDesc& d, int tile, int T, const TBShape& sh)
+{
+	using Op = OpDivergence<N>;
+	const Op op{N(d.c[0]), N(d.c[1]), N(d.c[2])};
+	const int nx = d.nx, ny = d.ny, ns = d.ns;
+	const int dxn = nx - 2, dyn = ny - 2, dzn = ns - 2;
+	const int tx = (dxn + sh.bx - 1) / sh.bx, ty = (dyn + sh.by - 1) / sh.by;
+	const int ix = tile % tx, iy = (tile / tx) % ty, iz = tile / (tx * ty);
+	const int x0 = 1 + ix * sh.bx, y0 = 1 + iy * sh.by, z0 = 1 + iz * sh.bz;
+	const int ex = min(sh.bx, 1 + dxn - x0), ey = min(sh.by, 1 + dyn - y0), ez = min(sh.bz, 1 + dzn - z0);
+	Ptrs<S> p{};
+	p.out[0] = (S*)d.a[0];
+	p.in[0] = (const S*)d.a[1];
+	p.in[1] = (const S*)d.a[2];
+	p.in[2] = (const S*)d.a[3];
+	const long long sy = nx, sz = (long long)nx * ny;
+	const int pe = ex * ey * ez;
+	for (int st = 0; st < T; st++)
+		for (int q = threadIdx.x; q < pe; q += kTBThreads) {
+			const int z = q / (ex * ey), rem = q - z * ex * ey, y = rem / ex, x = rem - y * ex;
+			const long long c = (x0 + x) + sy * (y0 + y) + sz * (z0 + z);
+			GAcc<N, S> at{p.in, c, sy, sz};
+			N o[3];
+			op.point(at, o);
+			p.out[0][c] = Conv<N, S>::to(o[0]);
+		}
+}
+
+// One launch of T steps over the blocks of every problem: read_b selects the
+// set read (0: the problems' own arrays, 1: the second set); the other set
+// is written.
+template <class N, class S>
+__global__ void __launch_bounds__(kTBThreads) batch_tb_kernel(const BatchDesc* __restrict__ desc, int nprob, int total,
+	const long long* __restrict__ step_base, int local, int T, TBShape sh, int read_b, int all_levels)
+{
+	// dynamic shared memory: the problems' first tiles, then the time levels
+	extern __shared__ __align__(16) unsigned char tb_smem[];
+	int* first = reinterpret_cast<int*>(tb_smem);
+	S* sm = reinterpret_cast<S*>(tb_smem + tb_first_bytes(nprob));
+	for (int q = threadIdx.x; q < nprob; q += kTBThreads) first[q] = desc[q].first;
+	__syncthreads();
+	const long long g = *step_base + local;
+	for (int item = blockIdx.x; item < total; item += gridDim.x) {
+		int lo = 0, hi = nprob - 1;
+		while (lo < hi) {
+			const int mid = (lo + hi + 1) >> 1;
+			if (first[mid] <= item) lo = mid;
+			else hi = mid - 1;
+		}
+		const BatchDesc& d = desc[lo];
+		const int t = item - d.first;
+		void* const* rd = read_b ? d.b : d.a;
+		void* const* wr = read_b ? d.a : d.b;
+		switch (d.stencil) {
+		case KG_LAPLACIAN:
+			tb_block<OpLaplacian<N>, N, S, 2>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, d, rd, wr, g, t, T, sh, sm,
+				all_levels != 0);
+			break;
+		case KG_GAUSSBLUR:
+			tb_block<OpGaussblur<N>, N, S, 2>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]), N(d.c[3]), N(d.c[4]),
+				N(d.c[5]), N(d.c[6])}, d, rd, wr, g, t, T, sh, sm, all_levels != 0);
+			break;
+		case KG_WAVE13PT:
+			tb_block<OpWave13pt<N>, N, S, 3>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, rd, wr, g, t, T, sh,
+				sm, all_levels != 0);
+			break;
+		case KG_DIVERGENCE:
+			tb_divergence<N, S>(d, t, T, sh);
+			break;
+		default: break;
+		}
+	}
+}
+
+// The rims (points outside the update domain; with `all`, every point) of
+// the rotating arrays of every problem copied from its own arrays into its
+// second set: CTAs per (problem, group of planes).
+template <class S>
+__global__ void batch_rim_copy(const BatchDesc* __restrict__ desc, int nprob, int all)
+{
+	for (int q = blockIdx.x; q < nprob; q += gridDim.x) {
+		const BatchDesc& d = desc[q];
+		int narr, r, k2d = 0;
+		switch (d.stencil) {
+		case KG_LAPLACIAN: narr = 2; r = 1; break;
+		case KG_GAUSSBLUR: narr = 2; r = 2; k2d = 1; break;
+		case KG_WAVE13PT: narr = 3; r = 2; break;
+		default: continue;
+		}
+		const int nx = d.nx, ny = d.ny, ns = d.ns;
+		const int rz = k2d ? 0 : r;
+		for (int z = blockIdx.y; z < ns; z += gridDim.y) {
+			const bool zrim = z < rz || z >= ns - rz;
+			for (int e = threadIdx.x; e < nx * ny; e += blockDim.x) {
+				const int y = e / nx, x = e - y * nx;
+				if (!all && !(zrim || y < r || y >= ny - r || x < r || x >= nx - r)) continue;
+				const long long c = e + (long long)nx * ny * z;
+				for (int k = 0; k < narr; k++) ((S*)d.b[k])[c] = ((const S*)d.a[k])[c];
+			}
+		}
+	}
+}
+
 __global__ void batch_advance(long long* step_base, int n)
 {
 	if (threadIdx.x == 0 && blockIdx.x == 0) *step_base += n;
 }
 
-// Tile shapes the tuner tries (BX, BY, KC).
+// Tile shapes the tuner tries (BX, BY, KC), one step per launch.
 struct Shape { int bx, by, kc; };
 static const Shape k_shapes[] = {{32, 8, 8}, {32, 4, 8}, {64, 4, 8}, {32, 8, 4}, {32, 8, 16}, {128, 2, 8},
 	{32, 8, 32}, {32, 16, 16}, {32, 4, 32}, {32, 8, 64}};
 static const int k_nshapes = sizeof(k_shapes) / sizeof(k_shapes[0]);
+// Temporal tiles (output block, steps per launch); configuration index
+// k_nshapes + i.  A shape whose shared memory a batch's stencils exceed is
+// not used for that batch.
+static const TBShape k_tb_shapes[] = {{32, 8, 8, 2}, {32, 8, 4, 2}, {32, 4, 4, 2}, {64, 4, 4, 2}, {64, 8, 4, 2},
+	{32, 8, 8, 3}, {32, 4, 4, 3}, {64, 4, 4, 3}, {32, 8, 8, 4}, {32, 4, 4, 4}};
+static const int k_ntb = sizeof(k_tb_shapes) / sizeof(k_tb_shapes[0]);
+static const int k_nconfigs = k_nshapes + k_ntb;
+// Steps each tuning trial times (a multiple of every temporal factor).
+constexpr int kTuneSteps = 12;
+constexpr int kSmemOptin = 227 * 1024;
 
 template <class N, class S>
 static cudaError_t launch_shape(int shape, dim3 grid, const BatchDesc* desc, int nprob, int total,
@@ -249,6 +563,47 @@ static int tiles_of(int stencil, int nx, int ny, int ns, const Shape& s, int* tx
 	return 0;
 }
 
+// Blocks of one problem for a temporal shape (2D: bx x (by bz) rows).
+static long long tb_tiles_of(int stencil, int nx, int ny, int ns, const TBShape& s)
+{
+	int r, k2d = 0;
+	switch (stencil) {
+	case KG_LAPLACIAN: case KG_DIVERGENCE: r = 1; break;
+	case KG_WAVE13PT: r = 2; break;
+	case KG_GAUSSBLUR: r = 2; k2d = 1; break;
+	default: return 0;
+	}
+	const long long dx = std::max(0, nx - 2 * r), dy = std::max(0, ny - 2 * r), dz = k2d ? 1 : std::max(0, ns - 2 * r);
+	const long long by = k2d ? (long long)s.by * s.bz : s.by, bz = k2d ? 1 : s.bz;
+	return ((dx + s.bx - 1) / s.bx) * ((dy + by - 1) / by) * ((dz + bz - 1) / bz);
+}
+
+// Dynamic shared memory of a temporal launch of T steps for these problems.
+static size_t tb_smem_bytes(const std::vector<kg_problem>& probs, int es, const TBShape& sh, int T)
+{
+	long long m = 0;
+	bool kinds[KG_NSTENCILS] = {false};
+	for (const kg_problem& p : probs) kinds[p.stencil] = true;
+	for (int k = 0; k < KG_NSTENCILS; k++)
+		if (kinds[k]) m = std::max(m, tb_smem_elems(k, sh, T));
+	return (size_t)tb_first_bytes((int)probs.size()) + (size_t)m * es;
+}
+
+template <class N, class S>
+static int tb_occupancy(size_t smem)
+{
+	static std::atomic<bool> set[64];   // the opt-in, once per device
+	int dev = 0;
+	cudaGetDevice(&dev);
+	if (dev >= 0 && dev < 64 && !set[dev].load(std::memory_order_acquire)) {
+		cudaFuncSetAttribute(batch_tb_kernel<N, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptin);
+		set[dev].store(true, std::memory_order_release);
+	}
+	int n = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_tb_kernel<N, S>, kTBThreads, smem);
+	return n;
+}
+
 }  // namespace kg
 
 using namespace kg;
@@ -265,12 +620,57 @@ struct kg_batch_s {
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	int graph_steps = 0;
+	void* scratch = nullptr;       // temporal tiles: the second set of the rotating arrays
+	size_t tb_smem = 0;            // temporal tiles: dynamic shared memory of a launch
 };
+
+static int es_of(const kg_batch_s* b) { return b->dtype == KG_F32 ? 4 : 8; }
+
+// The second set of every problem's rotating arrays (one allocation).
+static kg_status batch_scratch(kg_batch_s* b, std::vector<void*>* sets)
+{
+	const size_t es = (size_t)es_of(b);
+	size_t total = 0;
+	std::vector<size_t> off;
+	for (const kg_problem& p : b->probs) {
+		const int nrot = p.stencil == KG_WAVE13PT ? 3 : (p.stencil == KG_DIVERGENCE ? 0 : 2);
+		for (int k = 0; k < nrot; k++) {
+			off.push_back(total);
+			total += ((size_t)p.nx * p.ny * p.ns * es + 255) / 256 * 256;
+		}
+	}
+	if (!b->scratch && total) {
+		cudaError_t e = cudaMalloc(&b->scratch, total);
+		if (e != cudaSuccess) {
+			b->scratch = nullptr;
+			return fail_cuda(e, "kg_batch: second set of the rotating arrays");
+		}
+	}
+	sets->clear();
+	for (size_t o : off) sets->push_back((char*)b->scratch + o);
+	return KG_OK;
+}
 
 static kg_status batch_build_table(kg_batch_s* b, int shape)
 {
 	std::vector<BatchDesc> h(b->probs.size());
 	int first = 0;
+	const bool temporal = shape >= k_nshapes;
+	std::vector<void*> sets;
+	size_t next = 0;
+	if (temporal) {
+		const TBShape& sh = k_tb_shapes[shape - k_nshapes];
+		const size_t smem = tb_smem_bytes(b->probs, es_of(b), sh, sh.t);
+		if (smem > (size_t)kSmemOptin)
+			return fail(KG_EINVAL, "kg_batch: temporal shape %d needs %zu bytes of shared memory for these problems",
+				shape, smem);
+		kg_status s = batch_scratch(b, &sets);
+		if (s != KG_OK) return s;
+		// sets the shared-memory opt-in of the temporal kernel on this device
+		const int occ = b->dtype == KG_F32 ? tb_occupancy<FF, float>(smem) : tb_occupancy<SD, double>(smem);
+		if (occ < 1) return fail(KG_EINVAL, "kg_batch: temporal shape %d does not fit an SM", shape);
+		b->tb_smem = smem;
+	}
 	for (size_t q = 0; q < b->probs.size(); q++) {
 		const kg_problem& p = b->probs[q];
 		BatchDesc& d = h[q];
@@ -283,7 +683,16 @@ static kg_status batch_build_table(kg_batch_s* b, int shape)
 		if (p.stencil == KG_GAUSSBLUR)
 			d.c[6] = 1. / (p.coef[0] + 4 * (p.coef[1] + p.coef[2] + p.coef[3] + p.coef[5]) + 8 * p.coef[4]);
 		for (int k = 0; k < 4; k++) d.a[k] = p.arr[k];
-		tiles_of(p.stencil, p.nx, p.ny, p.ns, k_shapes[shape], &d.tiles_x, &d.tiles_y, &d.tiles_z);
+		if (temporal) {
+			const int nrot = p.stencil == KG_WAVE13PT ? 3 : (p.stencil == KG_DIVERGENCE ? 0 : 2);
+			for (int k = 0; k < nrot; k++) d.b[k] = sets[next++];
+			const long long t = tb_tiles_of(p.stencil, p.nx, p.ny, p.ns, k_tb_shapes[shape - k_nshapes]);
+			if (t > 0x7fffffffLL) return fail(KG_EINVAL, "kg_batch: more than 2^31 tiles");
+			d.tiles_x = (int)t;
+			d.tiles_y = d.tiles_z = 1;
+		} else {
+			tiles_of(p.stencil, p.nx, p.ny, p.ns, k_shapes[shape], &d.tiles_x, &d.tiles_y, &d.tiles_z);
+		}
 		d.first = first;
 		const long long nt = (long long)d.tiles_x * d.tiles_y * d.tiles_z;
 		if (first + nt > 0x7fffffffLL) return fail(KG_EINVAL, "kg_batch: more than 2^31 tiles");
@@ -296,10 +705,43 @@ static kg_status batch_build_table(kg_batch_s* b, int shape)
 	return KG_OK;
 }
 
+// A sequence of temporal launches: every launch reads one set of arrays and
+// writes the other, and the last writes the problems' own arrays, all of
+// their levels.  With an even number of launches the first reads the own
+// arrays, and the second set needs only their rims; with an odd number the
+// first reads the second set, which then gets a whole copy.
+template <class N, class S>
+static cudaError_t batch_tb_steps(kg_batch_s* b, int nsteps, cudaStream_t st)
+{
+	const TBShape sh = k_tb_shapes[b->shape - k_nshapes];
+	const int T = sh.t;
+	const int np = (int)b->probs.size();
+	const int nl = (nsteps + T - 1) / T;
+	batch_rim_copy<S><<<dim3((unsigned)std::min(np, 65535), 64), 256, 0, st>>>(b->d_desc, np, nl % 2);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	const dim3 grid(b->sms * b->ctas);
+	for (int i = 0; i < nl; i++) {
+		const int local = i * T, Ti = std::min(T, nsteps - local);
+		const int read_b = (nl - 1 - i) % 2 == 0 ? 1 : 0;
+		batch_tb_kernel<N, S><<<grid, kTBThreads, b->tb_smem, st>>>(b->d_desc, np, b->total, b->d_step, local, Ti, sh,
+			read_b, i == nl - 1 ? 1 : 0);
+		if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	}
+	return cudaSuccess;
+}
+
 static cudaError_t batch_launch_steps(kg_batch_s* b, int nsteps, cudaStream_t st)
 {
 	const dim3 grid(b->sms * b->ctas);
 	const int np = (int)b->probs.size();
+	if (b->shape >= k_nshapes) {
+		cudaError_t e = b->dtype == KG_F32 ? batch_tb_steps<FF, float>(b, nsteps, st)
+		                                   : batch_tb_steps<SD, double>(b, nsteps, st);
+		if (e != cudaSuccess) return e;
+		batch_advance<<<1, 32, 0, st>>>(b->d_step, nsteps);
+		return cudaGetLastError();
+	}
 	for (int s = 0; s < nsteps; s++) {
 		cudaError_t e = (b->dtype == KG_F32)
 			? launch_shape<FF, float>(b->shape, grid, b->d_desc, np, b->total, b->d_step, s, st)
@@ -382,7 +824,7 @@ kg_status kg_batch_create(kg_batch* out, const kg_problem* probs, int nprob)
 kg_status kg_batch_set_config(kg_batch b, int shape, int ctas_per_sm)
 {
 	clear_error();
-	if (!b || shape < 0 || shape >= k_nshapes || ctas_per_sm < 1 || ctas_per_sm > 32)
+	if (!b || shape < 0 || shape >= k_nconfigs || ctas_per_sm < 1 || ctas_per_sm > 32)
 		return fail(KG_EINVAL, "kg_batch_set_config: bad argument");
 	drop_graph(b);
 	b->ctas = ctas_per_sm;
@@ -394,12 +836,21 @@ kg_status kg_batch_get_config(kg_batch b, kg_batch_config* cfg)
 	clear_error();
 	if (!b || !cfg) return fail(KG_EINVAL, "kg_batch_get_config: bad argument");
 	cfg->shape = b->shape;
-	cfg->bx = k_shapes[b->shape].bx;
-	cfg->by = k_shapes[b->shape].by;
-	cfg->kc = k_shapes[b->shape].kc;
+	if (b->shape >= k_nshapes) {
+		const TBShape& t = k_tb_shapes[b->shape - k_nshapes];
+		cfg->bx = t.bx;
+		cfg->by = t.by;
+		cfg->kc = t.bz;
+		cfg->temporal = t.t;
+	} else {
+		cfg->bx = k_shapes[b->shape].bx;
+		cfg->by = k_shapes[b->shape].by;
+		cfg->kc = k_shapes[b->shape].kc;
+		cfg->temporal = 1;
+	}
 	cfg->ctas_per_sm = b->ctas;
 	cfg->tiles = b->total;
-	cfg->nshapes = k_nshapes;
+	cfg->nshapes = k_nconfigs;
 	cfg->steps_done = b->steps_done;
 	return KG_OK;
 }
@@ -461,7 +912,7 @@ kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream)
 			char key[256];
 			int shape, ctas;
 			while (fscanf(f, "%255s %d %d", key, &shape, &ctas) == 3) {
-				if (sig == key && shape >= 0 && shape < k_nshapes && ctas >= 1 && ctas <= 32) {
+				if (sig == key && shape >= 0 && shape < k_nconfigs && ctas >= 1 && ctas <= 32) {
 					fclose(f);
 					return kg_batch_set_config(b, shape, ctas);
 				}
@@ -478,16 +929,25 @@ kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream)
 	kg_status s = KG_OK;
 	// Each trial advances the batch; the roles stay consistent because the
 	// device step counter advances with them.
-	for (int sh = 0; sh < k_nshapes && s == KG_OK; sh++) {
+	for (int sh = 0; sh < k_nconfigs && s == KG_OK; sh++) {
 		// one wave of resident CTAs, one fewer per SM, half as many
-		const int occ = b->dtype == KG_F32 ? shape_occupancy<FF, float>(sh) : shape_occupancy<SD, double>(sh);
+		int occ;
+		if (sh < k_nshapes) {
+			occ = b->dtype == KG_F32 ? shape_occupancy<FF, float>(sh) : shape_occupancy<SD, double>(sh);
+		} else {
+			const TBShape& t = k_tb_shapes[sh - k_nshapes];
+			const size_t smem = tb_smem_bytes(b->probs, es_of(b), t, t.t);
+			if (smem > (size_t)kSmemOptin) continue;   // too large for these problems
+			occ = b->dtype == KG_F32 ? tb_occupancy<FF, float>(smem) : tb_occupancy<SD, double>(smem);
+			if (occ < 1) continue;
+		}
 		int cand[3] = {occ, occ > 1 ? occ - 1 : 1, occ > 1 ? occ / 2 : 1};
 		for (int c = 0; c < 3 && s == KG_OK; c++) {
 			if (c > 0 && (cand[c] == cand[c - 1] || (c == 2 && cand[2] == cand[0]))) continue;
 			if ((s = kg_batch_set_config(b, sh, cand[c])) != KG_OK) break;
 			if ((s = kg_batch_step(b, 1, stream)) != KG_OK) break;  // warm-up
 			cudaEventRecord(e0, st);
-			if ((s = kg_batch_step(b, 3, stream)) != KG_OK) break;
+			if ((s = kg_batch_step(b, kTuneSteps, stream)) != KG_OK) break;
 			cudaEventRecord(e1, st);
 			if ((s = fail_cuda(cudaEventSynchronize(e1), "kg_batch_tune")) != KG_OK) break;
 			float ms = 0;
@@ -548,6 +1008,7 @@ kg_status kg_batch_destroy(kg_batch b)
 	drop_graph(b);
 	cudaFree(b->d_desc);
 	cudaFree(b->d_step);
+	if (b->scratch) cudaFree(b->scratch);
 	delete b;
 	return KG_OK;
 }

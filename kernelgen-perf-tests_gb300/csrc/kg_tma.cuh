@@ -245,9 +245,24 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 // raised the CTA's abort flag; the thread then stops issuing and waits for
 // every copy it issued to land before it returns.  Normally it returns after
 // the compute warps are done with the last step.
-template <class Op, class S, class G>
+// The runs of one CTA of the TMA engine: planes kb, kb + gridDim.z kc, ...
+// (up to kc each) of its tile (xt, yt).
+struct ZRuns {
+	int xt, yt, kb, kend, kc;
+	__device__ __forceinline__ bool next(int& x, int& y, int& k0, int& n) {
+		if (kb >= kend) return false;
+		x = xt;
+		y = yt;
+		k0 = kb;
+		n = min(kc, kend - kb);
+		kb += gridDim.z * kc;
+		return true;
+	}
+};
+
+template <class Op, class S, class G, class Runs>
 __device__ __forceinline__ void tma_produce(const TMaps& maps, unsigned char* sm, uint64_t* full, uint64_t* done,
-	const volatile int* abort, int xt, int yt, int kend, int kc, int* err)
+	const volatile int* abort, Runs runs, int* err)
 {
 	constexpr int NB = G::NB, L = G::NB - 1;
 #pragma unroll
@@ -255,8 +270,8 @@ __device__ __forceinline__ void tma_produce(const TMaps& maps, unsigned char* sm
 		if (G::staged(q)) tma_prefetch_map(&maps.m[q]);
 	uint32_t g = 0, issued = 0;   // steps issued so far
 	bool ok = true;
-	for (int kb = Op::LZ + blockIdx.z * kc; kb < kend && ok; kb += gridDim.z * kc) {
-		const int nsteps = min(kc, kend - kb);
+	int xt, yt, kb, nsteps;
+	while (ok && runs.next(xt, yt, kb, nsteps)) {
 		// a new run's window may reuse any slot: wait for the previous run
 		if (g > 0) ok = mbar_wait(&done[(g - 1) % NB], ((g - 1) / NB) & 1, kTmaWaitCycles, abort);
 		for (int t = 0; t < nsteps && ok; t++) {
@@ -323,7 +338,8 @@ __global__ void __launch_bounds__(TX * TY + 32) tma_kernel(Op op, Ptrs<S> p, con
 	__syncthreads();
 
 	if (tid >= NC) {
-		if (tid == NC) tma_produce<Op, S, G>(maps, sm, full, done, abort, xt, yt, kend, kc, err);
+		if (tid == NC)
+			tma_produce<Op, S, G>(maps, sm, full, done, abort, ZRuns{xt, yt, Op::LZ + (int)blockIdx.z * kc, kend, kc}, err);
 		return;
 	}
 

@@ -16,6 +16,8 @@
 // arithmetic) whose reach along x is at most V on either side.
 #pragma once
 
+#include <algorithm>
+
 #include "kg_tma.cuh"
 
 namespace kg {
@@ -72,13 +74,36 @@ template <int I, int V, class F> __device__ __forceinline__ void for_v(F&& f)
 	}
 }
 
-// NW compute warps (one row of the tile each) and one producer warp; the
-// tile is 32 V columns x NW rows of every plane of a run along z.
+// The runs of one CTA of the vector engine.  The planes of all tiles are
+// numbered tile by tile (tile = column of the grid of BX x BY tiles, its
+// planes kz0 .. kz0 + dz - 1 one after the other) and CTA b takes the range
+// [b per, (b + 1) per): every CTA gets the same number of planes (to one),
+// in at most a few runs, however the tiles and the CTAs per wave divide.
+struct FlatRuns {
+	long long pos, end;
+	int dz, kz0, gx, bx, by, y0;
+	__device__ __forceinline__ bool next(int& x, int& y, int& k0, int& n) {
+		if (pos >= end) return false;
+		const long long tile = pos / dz;
+		const int kk = (int)(pos - tile * dz);
+		n = (int)min((long long)(dz - kk), end - pos);
+		x = (int)(tile % gx) * bx;
+		y = y0 + (int)(tile / gx) * by;
+		k0 = kz0 + kk;
+		pos += n;
+		return true;
+	}
+};
+
+// NW compute warps and one producer warp.  A warp owns RPW = 32 V / BX rows
+// of the tile (BX = 128 columns): lane l evaluates the V consecutive points
+// from column (l mod BX/V) V of row l / (BX/V), V = 16 bytes of storage.
 template <class Op, class N, class S, int V, int NW, int L>
 __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p, const __grid_constant__ TMaps maps,
-	int nx, int ny, int ns, int kc, int yt0, int* err, long long wait)
+	int nx, int ny, int ns, long long per_cta, int gx, int ntiles, int* err, long long wait)
 {
-	constexpr int BX = 32 * V, BY = NW, NC = 32 * NW;
+	constexpr int BX = 128, LPR = BX / V, RPW = 32 / LPR, BY = NW * RPW, NC = 32 * NW;
+	static_assert(LPR * RPW == 32, "a warp covers whole rows");
 	using G = TGeo<Op, S, BX, BY, L>;
 	constexpr int NB = G::NB;
 	constexpr Slots sl = Op::slots();
@@ -91,8 +116,10 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	volatile int* abort = reinterpret_cast<volatile int*>(sm + G::kAbort);
 
 	const int tid = threadIdx.x;
-	const int xt = blockIdx.x * BX, yt = Op::LY + (yt0 + (int)blockIdx.y) * BY;
-	const int kend = ns - Op::HZ;
+	const int dz = ns - Op::LZ - Op::HZ;
+	const long long total = (long long)ntiles * dz;
+	const long long b0 = (long long)blockIdx.x * per_cta;
+	FlatRuns runs{b0, min(total, b0 + per_cta), dz, Op::LZ, gx, BX, BY, Op::LY};
 
 	if (tid == 0) {
 		for (int b = 0; b < NB; b++) {
@@ -105,28 +132,29 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	__syncthreads();
 
 	if (tid >= NC) {
-		if (tid == NC) tma_produce<Op, S, G>(maps, sm, full, done, abort, xt, yt, kend, kc, err);
+		if (tid == NC) tma_produce<Op, S, G>(maps, sm, full, done, abort, runs, err);
 		return;
 	}
 
 	// ---- compute warps ----
 	const int lane = tid & 31, w = tid >> 5;
-	const int i0 = xt + lane * V, j = yt + w;
+	const int lx = lane % LPR, ry = w * RPW + lane / LPR;
 	const long long sy = nx, sz = (long long)nx * ny;
-	const bool row_ok = j < ny - Op::HY;
-	unsigned valid = 0;
-#pragma unroll
-	for (int v = 0; v < V; v++)
-		if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid |= 1u << v;
 	// byte offset of the lane's first column in the point's row of a plane, per input
 	int toff[6];
 #pragma unroll
 	for (int q = 0; q < G::NIN; q++)
-		toff[q] = ((w + Op::halo(q).y0) * G::W(q) + lane * V + G::XL(q)) * G::ES;
+		toff[q] = ((ry + Op::halo(q).y0) * G::W(q) + lx * V + G::XL(q)) * G::ES;
 
 	uint32_t g = 0;
-	for (int kb = Op::LZ + blockIdx.z * kc; kb < kend; kb += gridDim.z * kc) {
-		const int nsteps = min(kc, kend - kb);
+	int xt, yt, kb, nsteps;
+	while (runs.next(xt, yt, kb, nsteps)) {
+		const int i0 = xt + lx * V, j = yt + ry;
+		const bool row_ok = j < ny - Op::HY;
+		unsigned valid = 0;
+#pragma unroll
+		for (int v = 0; v < V; v++)
+			if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid |= 1u << v;
 		for (int s = 0; s < nsteps; s++) {
 			const int k = kb + s;
 			const uint32_t gs = g + s;
@@ -186,8 +214,8 @@ template <class Op, class S, int BX, int BY> struct TmaVecDepth {
 template <class Op, class N, class S>
 struct TmaVecLaunch {
 	static constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
-	static constexpr int V = 4, NW = 8;
-	static constexpr int BX = 32 * V, BY = NW;
+	static constexpr int V = 16 / (int)sizeof(S), NW = 8;
+	static constexpr int BX = 128, BY = NW * (32 * V / BX);
 	static constexpr int L = TmaVecDepth<Op, S, BX, BY>::L;
 	static constexpr int kThreads = 32 * NW + 32;
 	using G = TGeo<Op, S, BX, BY, L>;
@@ -197,7 +225,7 @@ struct TmaVecLaunch {
 		return true;
 	}
 	// built for 3D ops on 4- and 2-byte storage whose reach along x fits
-	static constexpr bool built = !k2d && sizeof(S) <= 4 && reach_ok();
+	static constexpr bool built = !k2d && (sizeof(S) == 4 || sizeof(S) == 2) && reach_ok();
 	static const void* func() {
 		if constexpr (built) return (const void*)tma_vec_kernel<Op, N, S, V, NW, L>;
 		else return nullptr;
@@ -256,15 +284,20 @@ struct TmaVecLaunch {
 				if (e != cudaSuccess) return e;
 			}
 			const int gx = (nx - Op::HX + BX - 1) / BX;
-			const int gy = (dy + BY - 1) / BY;
-			const int kc = tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX());
-			const int nz = (dz + kc - 1) / kc;
-			for (int y0 = 0; y0 < gy; y0 += 65535) {
-				dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
-				tma_vec_kernel<Op, N, S, V, NW, L><<<grid, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, kc, y0, err, wait);
-				if ((e = cudaGetLastError()) != cudaSuccess) return e;
-			}
-			return cudaSuccess;
+			const long long gy = (dy + BY - 1) / BY;
+			if ((long long)gx * gy > 0x7fffffffLL) return cudaErrorInvalidValue;
+			const int ntiles = (int)(gx * gy);
+			// the (tile, plane) pairs split evenly over one wave of CTAs, runs
+			// of at least kMinRun planes
+			constexpr long long kMinRun = 16;
+			const long long total = (long long)ntiles * dz;
+			long long ctas = std::min((long long)per_sm * sms, (total + kMinRun - 1) / kMinRun);
+			ctas = std::max(1LL, ctas);
+			const long long per = (total + ctas - 1) / ctas;
+			ctas = (total + per - 1) / per;
+			tma_vec_kernel<Op, N, S, V, NW, L><<<(unsigned)ctas, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, per,
+				gx, ntiles, err, wait);
+			return cudaGetLastError();
 		}
 	}
 };

@@ -122,6 +122,52 @@ def test_batch_every_tile_shape_and_tuning(tmp_path):
     b.close()
 
 
+def temporal_configs(b):
+    """Configuration indices of the temporal blocks (steps per launch > 1)."""
+    out = []
+    for shape in range(b.config().nshapes):
+        try:
+            b.set_config(shape, 2)
+        except kgb200.KgError:
+            continue            # its blocks need more shared memory than an SM has
+        if b.config().temporal > 1:
+            out.append((shape, b.config().temporal))
+    return out
+
+
+@pytest.mark.parametrize("dtype", [kgb200.KG_F32, kgb200.KG_F64])
+def test_batch_temporal_blocks_equal_individual_sweeps(dtype):
+    """Every temporal configuration, with step counts that leave a shorter
+    last launch and an odd or even number of launches, plain and replayed
+    from a graph: every array of every problem equals the problem's own
+    kg_sweep calls bit for bit."""
+    n = 40
+    probs, bufs, meta = make_batch(n, dtype, seed=17)
+    saved = [[a.clone() for a in arrs] for arrs in bufs]
+    ref = reference_run(meta, bufs, dtype, 11)
+    b = kgb200.Batch(probs)
+    configs = temporal_configs(b)
+    assert configs, "no temporal configuration fits"
+    for shape, t in configs:
+        for q in range(n):
+            for a, s in zip(bufs[q], saved[q]):
+                a.copy_(s)
+        b.set_config(shape, 1 + shape % 3)
+        b.set_step(0)
+        b.step(5)
+        b.capture(3)
+        b.launch()
+        b.launch()
+        torch.cuda.synchronize()
+        assert b.config().steps_done == 11
+        got = batch_final(b, bufs, n)
+        for q in range(n):
+            for k, (g, w) in enumerate(zip(got[q], ref[q])):
+                assert torch.equal(g, w), "config %d (T=%d) problem %d (%s) array %d differs" % (
+                    shape, t, q, meta[q][0], k)
+    b.close()
+
+
 def test_batch_f64_matches_oracle():
     probs, bufs, meta = make_batch(6, kgb200.KG_F64, seed=21)
     host = [[a.cpu().numpy().copy() for a in arrs] for arrs in bufs]
