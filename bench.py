@@ -352,6 +352,69 @@ def reference_final_means():
     return out
 
 
+# ---- bandwidth forms: FP32 and BF16 storage, one sweep ------------------------
+
+# Arrays read or written per sweep (the compulsory bytes are these times the
+# element size).
+ARRAYS_PER_PT = {"laplacian": 2, "divergence": 4, "gradient": 4, "uxx1": 6, "wave13pt": 3, "tricubic": 5,
+                 "tricubic2": 5, "jacobi": 2, "lapgsrb": 2, "gaussblur": 2, "gameoflife": 2}
+
+
+def run_bandwidth_forms(shape3=SHAPE3, reps=20):
+    """One sweep of every stencil in FP32 and in BF16 storage (FP32
+    arithmetic), engine chosen by the library, inputs uniform [-1,1) (uxx1's
+    density in [1,2)), timed with CUDA events over `reps` sweeps after three
+    warm-up sweeps; Gpts/s and the compulsory bytes per second against the
+    measured HBM peak.  Every array is larger than L2 at this size except the
+    2D tests' at 512x65536 FP32 (134 MB) and BF16 (67 MB)."""
+    import torch
+
+    hbm, kind = peaks()
+    lib = kgb200.load()
+    stream = torch.cuda.current_stream()
+    out = {"shape_3d": list(shape3), "shape_2d": list(SHAPE2), "peak_gbs": hbm, "peak_kind": kind}
+    for dname, dt, tdt, es in (("f32", kgb200.KG_F32, torch.float32, 4), ("bf16", kgb200.KG_BF16, torch.bfloat16, 2)):
+        row = {}
+        for name in SUITE:
+            if name == "gameoflife" and dt == kgb200.KG_BF16:
+                continue
+            sh = SHAPE2 if name in kgb200.IS2D else shape3
+            n = int(np_prod(sh))
+            narr = lib.kg_stencil_narrays(kgb200.STENCIL_ID[name])
+            gen = torch.Generator(device="cuda")
+            gen.manual_seed(7)
+            bufs = [(torch.rand(n, generator=gen, device="cuda") * 2 - 1).to(tdt) for _ in range(narr)]
+            if name == "uxx1":
+                bufs[2] = (1.5 + 0.5 * bufs[2].float()).to(tdt)
+            coef = [0.5, 0.1, 0.05, 0.02, 0.01, 0.3][:lib.kg_stencil_ncoefs(kgb200.STENCIL_ID[name])]
+            ptrs = [b.data_ptr() for b in bufs]
+            seq = []
+            for _ in range(6):
+                seq.append(kgb200.problem(name, dt, sh, coef, ptrs))
+                ptrs = kgb200.rotate(name, ptrs)
+            sp = kgb200.stream_ptr(stream)
+            for r in range(3):
+                kgb200.check(lib.kg_sweep(ctypes.byref(seq[r % 6]), sp))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for r in range(reps):
+                kgb200.check(lib.kg_sweep(ctypes.byref(seq[r % 6]), sp))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            kgb200.engine_status(stream)
+            ms = e0.elapsed_time(e1) / reps
+            gbs = ARRAYS_PER_PT[name] * es * n / (ms * 1e-3) / 1e9
+            row[name] = {"ms_per_sweep": round(ms, 4), "gpts": round(n / (ms * 1e-3) / 1e9, 1),
+                         "hbm_gbs": round(gbs, 1), "hbm_frac_of_measured": round(gbs / hbm, 3)}
+            del bufs
+        out[dname] = row
+        torch.cuda.empty_cache()
+    out["bf16_over_f32_gpts"] = {n: round(out["bf16"][n]["gpts"] / out["f32"][n]["gpts"], 2)
+                                 for n in out["bf16"] if n in out["f32"]}
+    return out
+
+
 # ---- the full-suite workload's project-defined inputs ----------------------
 
 def run_project_inits(reps=5):
@@ -976,9 +1039,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision-sweep summary")
-    ap.add_argument("--workload", default="suite", choices=["suite", "precision", "batched", "ir"])
+    ap.add_argument("--workload", default="suite", choices=["suite", "precision", "batched", "ir", "bandwidth"])
     ap.add_argument("--ir-shape", default="768,768,512")
     ap.add_argument("--ir-fp64-cap", type=int, default=0, help="sweep cap of the FP64 SOR run (0: none)")
+    ap.add_argument("--ir-jacobi-cap", type=int, default=0,
+                    help="sweep cap of the refinement run with FP32 Jacobi sweeps (0: not run)")
     args = ap.parse_args()
     args.world, args.rank, args.local_rank = dist_env()
     if args.impl == "reference":
@@ -995,7 +1060,11 @@ def main():
     dtype = kgb200.DTYPES[args.dtype]
     if args.workload == "ir":
         shape = tuple(int(v) for v in args.ir_shape.split(","))
-        res = run_ir(shape, fp64_cap=args.ir_fp64_cap or None)
+        kinds = [("fp64_sor", kgb200.KG_SOLVE_SOR_F64, args.ir_fp64_cap or None),
+                 ("ir_fp32_sor", kgb200.KG_SOLVE_IR_SOR_F32, None)]
+        if args.ir_jacobi_cap:
+            kinds.append(("ir_fp32_jacobi", kgb200.KG_SOLVE_IR_JACOBI_F32, args.ir_jacobi_cap))
+        res = run_ir(shape, kinds=kinds)
         if args.rank == 0:
             print(json.dumps({"workload": "mixed-precision iterative refinement, Poisson 7-point", "forms": res}))
         return 0
@@ -1004,6 +1073,11 @@ def main():
         if args.rank == 0:
             print(json.dumps({"workload": "batched: 256 problems, log-uniform sizes in [32,256], "
                               "{laplacian, divergence, wave13pt, gaussblur}, FP32, 50 steps", "forms": res}))
+        return 0
+    if args.workload == "bandwidth":
+        res = run_bandwidth_forms()
+        if args.rank == 0:
+            print(json.dumps({"workload": "FP32 and BF16 storage, one sweep per stencil", "forms": res}))
         return 0
     if args.workload == "precision":
         res = run_precision()
@@ -1111,9 +1185,12 @@ def main():
             **run_precision())}
         line["forms"]["batched"] = run_batched(tune_cache=os.environ.get("KG_TUNE_CACHE"))
         line["project_inits"] = run_project_inits()
+        line["forms"]["bandwidth"] = run_bandwidth_forms()
         line["forms"]["iterative_refinement"] = dict(
             note="measured to tolerance on 192x192x128; the 768x768x512 run is bench.py --workload ir",
-            **run_ir(IR_SMALL))
+            **run_ir(IR_SMALL, kinds=[("fp64_sor", kgb200.KG_SOLVE_SOR_F64, None),
+                                      ("ir_fp32_sor", kgb200.KG_SOLVE_IR_SOR_F32, None),
+                                      ("ir_fp32_jacobi", kgb200.KG_SOLVE_IR_JACOBI_F32, 400000)]))
         line["other_tests"] = run_other()
     if args.rank == 0 and args.world == 1 and not args.no_cpu:
         cpu = CpuSuite()

@@ -74,33 +74,12 @@ template <int I, int V, class F> __device__ __forceinline__ void for_v(F&& f)
 	}
 }
 
-// The runs of one CTA of the vector engine.  The planes of all tiles are
-// numbered tile by tile (tile = column of the grid of BX x BY tiles, its
-// planes kz0 .. kz0 + dz - 1 one after the other) and CTA b takes the range
-// [b per, (b + 1) per): every CTA gets the same number of planes (to one),
-// in at most a few runs, however the tiles and the CTAs per wave divide.
-struct FlatRuns {
-	long long pos, end;
-	int dz, kz0, gx, bx, by, y0;
-	__device__ __forceinline__ bool next(int& x, int& y, int& k0, int& n) {
-		if (pos >= end) return false;
-		const long long tile = pos / dz;
-		const int kk = (int)(pos - tile * dz);
-		n = (int)min((long long)(dz - kk), end - pos);
-		x = (int)(tile % gx) * bx;
-		y = y0 + (int)(tile / gx) * by;
-		k0 = kz0 + kk;
-		pos += n;
-		return true;
-	}
-};
-
 // NW compute warps and one producer warp.  A warp owns RPW = 32 V / BX rows
 // of the tile (BX = 128 columns): lane l evaluates the V consecutive points
 // from column (l mod BX/V) V of row l / (BX/V), V = 16 bytes of storage.
 template <class Op, class N, class S, int V, int NW, int L>
 __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p, const __grid_constant__ TMaps maps,
-	int nx, int ny, int ns, long long per_cta, int gx, int ntiles, int* err, long long wait)
+	int nx, int ny, int ns, int kc, int yt0, int* err, long long wait)
 {
 	constexpr int BX = 128, LPR = BX / V, RPW = 32 / LPR, BY = NW * RPW, NC = 32 * NW;
 	static_assert(LPR * RPW == 32, "a warp covers whole rows");
@@ -116,10 +95,10 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	volatile int* abort = reinterpret_cast<volatile int*>(sm + G::kAbort);
 
 	const int tid = threadIdx.x;
-	const int dz = ns - Op::LZ - Op::HZ;
-	const long long total = (long long)ntiles * dz;
-	const long long b0 = (long long)blockIdx.x * per_cta;
-	FlatRuns runs{b0, min(total, b0 + per_cta), dz, Op::LZ, gx, BX, BY, Op::LY};
+	const int xt = blockIdx.x * BX, yt = Op::LY + (yt0 + (int)blockIdx.y) * BY;
+	const int kend = ns - Op::HZ;
+	// the CTA's runs along z (each run is a window plus steps of planes)
+	const ZRuns runs{xt, yt, Op::LZ + (int)blockIdx.z * kc, kend, kc};
 
 	if (tid == 0) {
 		for (int b = 0; b < NB; b++) {
@@ -146,15 +125,16 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	for (int q = 0; q < G::NIN; q++)
 		toff[q] = ((ry + Op::halo(q).y0) * G::W(q) + lx * V + G::XL(q)) * G::ES;
 
-	uint32_t g = 0;
-	int xt, yt, kb, nsteps;
-	while (runs.next(xt, yt, kb, nsteps)) {
-		const int i0 = xt + lx * V, j = yt + ry;
-		const bool row_ok = j < ny - Op::HY;
-		unsigned valid = 0;
+	const int i0 = xt + lx * V, j = yt + ry;
+	const bool row_ok = j < ny - Op::HY;
+	unsigned valid = 0;
 #pragma unroll
-		for (int v = 0; v < V; v++)
-			if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid |= 1u << v;
+	for (int v = 0; v < V; v++)
+		if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid |= 1u << v;
+	uint32_t g = 0;
+	ZRuns rz = runs;
+	int xr, yr, kb, nsteps;
+	while (rz.next(xr, yr, kb, nsteps)) {
 		for (int s = 0; s < nsteps; s++) {
 			const int k = kb + s;
 			const uint32_t gs = g + s;
@@ -284,20 +264,18 @@ struct TmaVecLaunch {
 				if (e != cudaSuccess) return e;
 			}
 			const int gx = (nx - Op::HX + BX - 1) / BX;
-			const long long gy = (dy + BY - 1) / BY;
-			if ((long long)gx * gy > 0x7fffffffLL) return cudaErrorInvalidValue;
-			const int ntiles = (int)(gx * gy);
-			// the (tile, plane) pairs split evenly over one wave of CTAs, runs
-			// of at least kMinRun planes
-			constexpr long long kMinRun = 16;
-			const long long total = (long long)ntiles * dz;
-			long long ctas = std::min((long long)per_sm * sms, (total + kMinRun - 1) / kMinRun);
-			ctas = std::max(1LL, ctas);
-			const long long per = (total + ctas - 1) / ctas;
-			ctas = (total + per - 1) / per;
-			tma_vec_kernel<Op, N, S, V, NW, L><<<(unsigned)ctas, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, per,
-				gx, ntiles, err, wait);
-			return cudaGetLastError();
+			const int gy = (dy + BY - 1) / BY;
+			// z split into runs so that the CTAs fill whole waves (all tiles
+			// then walk the same planes at about the same time, and the halo
+			// rows of neighbouring tiles are served from L2)
+			const int kc = tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX());
+			const int nz = (dz + kc - 1) / kc;
+			for (int y0 = 0; y0 < gy; y0 += 65535) {
+				dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
+				tma_vec_kernel<Op, N, S, V, NW, L><<<grid, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, kc, y0, err, wait);
+				if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			}
+			return cudaSuccess;
 		}
 	}
 };

@@ -102,7 +102,12 @@ def test_batch_every_tile_shape_and_tuning(tmp_path):
         for q in range(n):
             for a, s in zip(bufs[q], saved[q]):
                 a.copy_(s)
-        b.set_config(shape, 2 + shape % 3)
+        try:
+            b.set_config(shape, 2 + shape % 3)
+        except kgb200.KgError as e:
+            # a temporal block too large for the shared memory of an SM
+            assert "shared memory" in str(e)
+            continue
         b.set_step(0)
         b.step(4)
         torch.cuda.synchronize()
