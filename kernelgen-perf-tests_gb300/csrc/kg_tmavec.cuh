@@ -36,16 +36,16 @@ __device__ __forceinline__ S vrow_load(const unsigned char* b, int row_elems, in
 	return pk.v[x % V];
 }
 
-template <class Op, class N, class S, class G, int V, int VI> struct VAcc {
+template <class Op, class N, class S, class G, int V, int VI, int RY = 0> struct VAcc {
 	static constexpr int ZS = 5;
 	const unsigned char* (*base)[ZS];   // per input and dz + z0: the lane's first column in the point's row
 	const S* const* in;
 	long long c, sy, sz;                      // c: the lane's first point
 	__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
-		return Conv<N, S>::from(vrow_load<S, V>(base[q][dz + Op::halo(q).z0], dy * G::W(q), VI + dx + V));
+		return Conv<N, S>::from(vrow_load<S, V>(base[q][dz + Op::halo(q).z0], (dy + RY) * G::W(q), VI + dx + V));
 	}
 	__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
-		return __ldg(in[q] + c + VI + dx + dy * sy + dz * sz);
+		return __ldg(in[q] + c + VI + dx + (dy + RY) * sy + dz * sz);
 	}
 };
 
@@ -74,19 +74,21 @@ template <int I, int V, class F> __device__ __forceinline__ void for_v(F&& f)
 	}
 }
 
-// NW compute warps and one producer warp.  A warp owns RPW = 32 V / BX rows
-// of the tile (BX = 128 columns): lane l evaluates the V consecutive points
-// from column (l mod BX/V) V of row l / (BX/V), V = 16 bytes of storage.
-template <class Op, class N, class S, int V, int NW, int L>
+// NW compute warps and one producer warp.  The warps cover RB = NW RPW rows
+// of the tile (BX = 128 columns, RPW = 32 V / BX rows per warp): lane l
+// evaluates the V consecutive points from column (l mod BX/V) V of row
+// l / (BX/V) of its warp's rows, V = 16 bytes of storage, and the same
+// points PY - 1 more times, RB rows further down each time (BY = RB PY).
+template <class Op, class N, class S, int V, int NW, int PY, int L>
 __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p, const __grid_constant__ TMaps maps,
 	int nx, int ny, int ns, int kc, int yt0, int* err, long long wait)
 {
-	constexpr int BX = 128, LPR = BX / V, RPW = 32 / LPR, BY = NW * RPW, NC = 32 * NW;
+	constexpr int BX = 128, LPR = BX / V, RPW = 32 / LPR, RB = NW * RPW, BY = RB * PY, NC = 32 * NW;
 	static_assert(LPR * RPW == 32, "a warp covers whole rows");
 	using G = TGeo<Op, S, BX, BY, L>;
 	constexpr int NB = G::NB;
 	constexpr Slots sl = Op::slots();
-	constexpr int ZS = VAcc<Op, N, S, G, V, 0>::ZS;
+	constexpr int ZS = VAcc<Op, N, S, G, V, 0, 0>::ZS;
 	static_assert(G::fits(), "tile does not fit the TMA engine");
 	static_assert(G::NZMAX() <= ZS, "at most ZS planes per window");
 	extern __shared__ __align__(128) unsigned char sm[];
@@ -126,11 +128,15 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 		toff[q] = ((ry + Op::halo(q).y0) * G::W(q) + lx * V + G::XL(q)) * G::ES;
 
 	const int i0 = xt + lx * V, j = yt + ry;
-	const bool row_ok = j < ny - Op::HY;
-	unsigned valid = 0;
+	unsigned valid[PY];
 #pragma unroll
-	for (int v = 0; v < V; v++)
-		if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid |= 1u << v;
+	for (int r = 0; r < PY; r++) {
+		const bool row_ok = j + r * RB < ny - Op::HY;
+		valid[r] = 0;
+#pragma unroll
+		for (int v = 0; v < V; v++)
+			if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid[r] |= 1u << v;
+	}
 	uint32_t g = 0;
 	ZRuns rz = runs;
 	int xr, yr, kb, nsteps;
@@ -157,22 +163,27 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 						base[q][d] = sm + G::offset(q) + G::step_slot(q, s0, d - h.z0) * G::PS(q) + toff[q];
 			}
 			const long long c = i0 + sy * j + sz * k;
-			S o[3][V];
-			for_v<0, V>([&](auto vi) {
-				constexpr int VI = decltype(vi)::value;
-				VAcc<Op, N, S, G, V, VI> at{base, p.in, c, sy, sz};
-				N r[3];
-				op.point(at, r);
+			S o[PY][3][V];
+			for_v<0, PY>([&](auto ri) {
+				constexpr int R = decltype(ri)::value;
+				for_v<0, V>([&](auto vi) {
+					constexpr int VI = decltype(vi)::value;
+					VAcc<Op, N, S, G, V, VI, R * RB> at{base, p.in, c, sy, sz};
+					N r[3];
+					op.point(at, r);
 #pragma unroll
-				for (int q = 0; q < sl.nout; q++) o[q][VI] = Conv<N, S>::to(r[q]);
+					for (int q = 0; q < sl.nout; q++) o[R][q][VI] = Conv<N, S>::to(r[q]);
+				});
 			});
 			// this warp is done with the step's planes
 			__syncwarp();
 			if (lane == 0) mbar_arrive(&done[gs % NB]);
-			if (valid) {
 #pragma unroll
-				for (int q = 0; q < sl.nout; q++) vstore<S, V>(p.out[q] + c, o[q], valid);
-			}
+			for (int r = 0; r < PY; r++)
+				if (valid[r]) {
+#pragma unroll
+					for (int q = 0; q < sl.nout; q++) vstore<S, V>(p.out[q] + c + r * RB * sy, o[r][q], valid[r]);
+				}
 		}
 		g += nsteps;
 	}
@@ -184,6 +195,10 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 #ifndef KG_TMAVEC_BUDGET
 #define KG_TMAVEC_BUDGET (100 * 1024)
 #endif
+// Rows of points per lane (each lane evaluates PY x V points per plane).
+#ifndef KG_TMAVEC_PY
+#define KG_TMAVEC_PY 1
+#endif
 template <class Op, class S, int BX, int BY> struct TmaVecDepth {
 	template <int L> static constexpr int bytes() { return TGeo<Op, S, BX, BY, L>::total(); }
 	static constexpr int kBudget = KG_TMAVEC_BUDGET;
@@ -194,8 +209,8 @@ template <class Op, class S, int BX, int BY> struct TmaVecDepth {
 template <class Op, class N, class S>
 struct TmaVecLaunch {
 	static constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
-	static constexpr int V = 16 / (int)sizeof(S), NW = 8;
-	static constexpr int BX = 128, BY = NW * (32 * V / BX);
+	static constexpr int V = 16 / (int)sizeof(S), NW = 8, PY = KG_TMAVEC_PY;
+	static constexpr int BX = 128, BY = NW * (32 * V / BX) * PY;
 	static constexpr int L = TmaVecDepth<Op, S, BX, BY>::L;
 	static constexpr int kThreads = 32 * NW + 32;
 	using G = TGeo<Op, S, BX, BY, L>;
@@ -207,7 +222,7 @@ struct TmaVecLaunch {
 	// built for 3D ops on 4- and 2-byte storage whose reach along x fits
 	static constexpr bool built = !k2d && (sizeof(S) == 4 || sizeof(S) == 2) && reach_ok();
 	static const void* func() {
-		if constexpr (built) return (const void*)tma_vec_kernel<Op, N, S, V, NW, L>;
+		if constexpr (built) return (const void*)tma_vec_kernel<Op, N, S, V, NW, PY, L>;
 		else return nullptr;
 	}
 
@@ -247,7 +262,7 @@ struct TmaVecLaunch {
 					return e;
 				int b = 0, n = 0;
 				if ((e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-				if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, tma_vec_kernel<Op, N, S, V, NW, L>, kThreads, smem)) != cudaSuccess)
+				if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, tma_vec_kernel<Op, N, S, V, NW, PY, L>, kThreads, smem)) != cudaSuccess)
 					return e;
 				occ = ((b > 0 ? b : 1) << 16) | (n & 0xffff);
 				occ_of[dev].store(occ, std::memory_order_release);
@@ -272,7 +287,7 @@ struct TmaVecLaunch {
 			const int nz = (dz + kc - 1) / kc;
 			for (int y0 = 0; y0 < gy; y0 += 65535) {
 				dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
-				tma_vec_kernel<Op, N, S, V, NW, L><<<grid, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, kc, y0, err, wait);
+				tma_vec_kernel<Op, N, S, V, NW, PY, L><<<grid, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, kc, y0, err, wait);
 				if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			}
 			return cudaSuccess;
