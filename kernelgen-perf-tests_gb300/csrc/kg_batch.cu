@@ -47,6 +47,7 @@
 #define KG_SUMS_ON_FP64_UNIT 1
 #include "kg_engine.cuh"
 #include "kg_internal.h"
+#include "kg_tma.cuh"
 
 namespace kg {
 
@@ -464,6 +465,300 @@ __global__ void batch_rim_copy(const BatchDesc* __restrict__ desc, int nprob, in
 				const long long c = e + (long long)nx * ny * z;
 				for (int k = 0; k < narr; k++) ((S*)d.b[k])[c] = ((const S*)d.a[k])[c];
 			}
+		}
+	}
+}
+
+// ---- bulk-staged tiles ---------------------------------------------------------
+//
+// The one-step tile of the batch (NT consecutive (i, j) columns of a problem,
+// KC planes; 2D: KC groups of NT columns), with its inputs staged in shared
+// memory by bulk copies instead of read through L1.  The NT columns of a
+// plane lie in one contiguous range of the array, grown by the input's reach
+// (x0 + y0 nx before, x1 + y1 nx after): one 1D bulk copy per input and plane
+// (cp.async.bulk, 16-byte aligned, rounded out to 16 bytes and never past the
+// array's last whole 16 bytes).  A producer warp issues each step's copies
+// kBulkL steps ahead of the compute warps, onto an mbarrier per step (as the
+// TMA engine does, with its bounded waits and drain); each input keeps a ring
+// of NZ + kBulkL plane ranges.  The batch's small problems are bound by the
+// latency of their loads; the copies put several steps of loads in flight
+// without taking registers.  A step whose range the array's end cut short
+// reads its inputs from global memory instead (the last up to 15 bytes of an
+// array).  Every point is the same body as the other engines evaluate.
+
+constexpr int kBulkL = 3;              // steps of copies in flight
+constexpr int kBulkNB = kBulkL + 1;    // mbarriers per direction
+constexpr int kBulkBar = 128;          // bytes: 2 x kBulkNB mbarriers, the abort flag
+
+// Shared-memory rings of one stencil's inputs: elements per slot, byte offset.
+struct BulkRings {
+	int cap[4];
+	int off[4];
+};
+struct BulkLayout {
+	BulkRings k[4];    // laplacian, divergence, wave13pt, gaussblur (stencil ids 0, 1, 4, 9)
+};
+__host__ __device__ __forceinline__ int bulk_kind(int stencil)
+{
+	return stencil == KG_LAPLACIAN ? 0 : stencil == KG_DIVERGENCE ? 1 : stencil == KG_WAVE13PT ? 2 : 3;
+}
+
+__device__ __forceinline__ void bulk_copy(void* dst_smem, const void* src, unsigned bytes, uint64_t* bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+		::"r"(smem_addr(dst_smem)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+
+// One item (tile) of the batch as the bulk kernel walks it.
+template <class Op> struct BulkItem {
+	static constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
+	int nx, ny, ns, dxn;
+	long long ncol, col0, P;
+	int kb, nsteps;
+	__device__ __forceinline__ void init(const BatchDesc& d, int t, int NT, int KC) {
+		nx = d.nx;
+		ny = d.ny;
+		ns = d.ns;
+		dxn = nx - Op::LX - Op::HX;
+		ncol = (long long)dxn * (ny - Op::LY - Op::HY);
+		P = (long long)nx * ny;
+		const int tcol = t % d.tiles_x, tz = t / d.tiles_x;
+		if (k2d) {
+			col0 = (long long)tcol * KC * NT;
+			kb = 0;
+			nsteps = (int)min((long long)KC, (ncol - col0 + NT - 1) / NT);
+		} else {
+			col0 = (long long)tcol * NT;
+			kb = Op::LZ + tz * KC;
+			nsteps = min(KC, ns - Op::HZ - kb);
+		}
+	}
+	// full index (in its plane) of interior column col (the bulk path takes
+	// problems of fewer than 2^31 points, so 32-bit division suffices)
+	__device__ __forceinline__ long long f(long long col) const {
+		const int c = (int)col, j = c / dxn;
+		return Op::LX + (c - j * dxn) + (long long)nx * (Op::LY + j);
+	}
+};
+
+// The chunk of input q of Op for a step: the element range [st, st + count)
+// it copies, the 16-byte phase of its first needed element, and whether the
+// array's end cut it short.
+template <class Op, class S> struct BulkChunk {
+	long long st;
+	int count, phase;
+	bool cut;
+	__device__ __forceinline__ void make(int q, long long fl, long long fh, long long pbase, int nx, long long n) {
+		constexpr int A = 16 / (int)sizeof(S);
+		const Halo h = Op::halo(q);
+		const long long lo = fl - (h.x0 + (long long)h.y0 * nx) + pbase;
+		const long long end = fh + h.x1 + (long long)h.y1 * nx + 1 + pbase;   // exclusive
+		const long long nfl = n / A * A;
+		phase = (int)(lo & (A - 1));
+		st = lo - phase;
+		const long long e = min((end + A - 1) / A * A, nfl);
+		count = (int)max(0LL, e - st);
+		cut = end > nfl || count == 0;
+	}
+};
+
+template <class Op, class N, class S, int NT, int KC>
+__device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>& p, const BulkRings& rg,
+	unsigned char* sm, uint64_t* full, uint64_t* done, volatile int* abort, uint32_t& g, bool producer, int* err,
+	long long wait, bool& ok)
+{
+	constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
+	constexpr Slots sl = Op::slots();
+	constexpr int NIN = sl.nin;
+	constexpr int ES = (int)sizeof(S);
+	BulkItem<Op> it;
+	it.init(d, t, NT, KC);
+	const long long n = it.P * it.ns;
+	auto NZ = [](int q) { return k2d ? 1 : Op::halo(q).z0 + Op::halo(q).z1 + 1; };
+	auto RZ = [&](int q) { return NZ(q) + kBulkL; };
+	// the range of step s: columns and plane
+	auto step_cols = [&](int s, long long& fl, long long& fh) {
+		const long long c0 = k2d ? it.col0 + (long long)s * NT : it.col0;
+		const long long c1 = min(c0 + NT, it.ncol) - 1;
+		fl = it.f(c0);
+		fh = it.f(c1);
+	};
+	if (producer) {
+		// a new item's windows may reuse any slot: wait for the previous item
+		if (g > 0 && ok) ok = mbar_wait(&done[(g - 1) % kBulkNB], ((g - 1) / kBulkNB) & 1, kTmaWaitCycles, abort);
+		uint32_t issued = g;
+		for (int s = 0; s < it.nsteps && ok; s++) {
+			const uint32_t gs = g + s;
+			if (s >= kBulkL + 1)
+				ok = mbar_wait(&done[(gs - kBulkL - 1) % kBulkNB], ((gs - kBulkL - 1) / kBulkNB) & 1, kTmaWaitCycles, abort);
+			if (!ok) break;
+			long long fl, fh;
+			step_cols(s, fl, fh);
+			const int k = it.kb + s;
+			// planes of this step: the window at the first step, then the newest
+			unsigned bytes = 0;
+			BulkChunk<Op, S> ch[6][5];
+			int np[6], p0[6];
+#pragma unroll
+			for (int q = 0; q < NIN; q++) {
+				const Halo h = Op::halo(q);
+				p0[q] = k2d ? 0 : (s == 0 ? k - h.z0 : k + h.z1);
+				np[q] = k2d ? 1 : (s == 0 ? NZ(q) : 1);
+				for (int m = 0; m < np[q]; m++) {
+					ch[q][m].make(q, fl, fh, k2d ? 0 : (long long)(p0[q] + m) * it.P, it.nx, n);
+					bytes += (unsigned)ch[q][m].count * ES;
+				}
+			}
+			mbar_expect_tx(&full[gs % kBulkNB], bytes);
+			fence_proxy_async();
+#pragma unroll
+			for (int q = 0; q < NIN; q++)
+				for (int m = 0; m < np[q]; m++) {
+					const int slot = (k2d ? s : p0[q] + m) % RZ(q);
+					if (ch[q][m].count > 0)
+						bulk_copy(sm + rg.off[q] + slot * rg.cap[q] * ES, p.in[q] + ch[q][m].st,
+							(unsigned)ch[q][m].count * ES, &full[gs % kBulkNB]);
+				}
+			issued = gs + 1;
+		}
+		if (!ok) {
+			// every step before the last kBulkNB issued is done; the copies of
+			// those land before the CTA's shared memory goes away
+			atomicExch(err, 1);
+			for (uint32_t w = issued > kBulkNB ? issued - kBulkNB : 0; w < issued; w++)
+				mbar_wait(&full[w % kBulkNB], (w / kBulkNB) & 1, kTmaWaitCycles);
+		}
+		g += it.nsteps;
+		return;
+	}
+	// ---- compute warps ----
+	const int tid = threadIdx.x, lane = tid & 31;
+	for (int s = 0; s < it.nsteps; s++) {
+		const uint32_t gs = g + s;
+		const bool got = __all_sync(0xffffffffu, mbar_wait(&full[gs % kBulkNB], (gs / kBulkNB) & 1, wait, abort));
+		if (!got) {
+			if (lane == 0) {
+				*abort = 1;
+				atomicExch(err, 1);
+			}
+			ok = false;
+			return;
+		}
+		long long fl, fh;
+		step_cols(s, fl, fh);
+		const long long c0 = k2d ? it.col0 + (long long)s * NT : it.col0;
+		const long long col = c0 + tid;
+		const int k = it.kb + s;
+		if (col < it.ncol) {
+			const long long fc = it.f(col);
+			const long long pk = k2d ? 0 : (long long)k * it.P;
+			bool cut = false;
+			// byte address of the point's own element in each (input, plane) slot
+			const unsigned char* a[6][5];
+#pragma unroll
+			for (int q = 0; q < NIN; q++) {
+				const Halo h = Op::halo(q);
+#pragma unroll
+				for (int m = 0; m < 5; m++) {
+					if (m >= NZ(q)) continue;
+					const int pl = k2d ? 0 : k - h.z0 + m;
+					BulkChunk<Op, S> ch;
+					ch.make(q, fl, fh, k2d ? 0 : (long long)pl * it.P, it.nx, n);
+					cut = cut || ch.cut;
+					const int slot = (k2d ? s : pl) % RZ(q);
+					const long long rel = fc - fl + (h.x0 + (long long)h.y0 * it.nx) + ch.phase;
+					a[q][m] = sm + rg.off[q] + slot * rg.cap[q] * ES + rel * ES;
+				}
+			}
+			N o[3];
+			if (!cut) {
+				struct Acc {
+					const unsigned char* (*a)[5];
+					int nx;
+					__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
+						return Conv<N, S>::from(*reinterpret_cast<const S*>(a[q][dz + Op::halo(q).z0] + (dx + dy * nx) * ES));
+					}
+					__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
+						return *reinterpret_cast<const S*>(a[q][dz + Op::halo(q).z0] + (dx + dy * nx) * ES);
+					}
+				} at{a, it.nx};
+				op.point(at, o);
+			} else {
+				GAcc<N, S> at{p.in, fc + pk, it.nx, it.P};
+				op.point(at, o);
+			}
+#pragma unroll
+			for (int q = 0; q < sl.nout; q++) p.out[q][fc + pk] = Conv<N, S>::to(o[q]);
+		}
+		__syncwarp();
+		if (lane == 0) mbar_arrive(&done[gs % kBulkNB]);
+	}
+	g += it.nsteps;
+}
+
+template <class N, class S, int NT, int KC>
+__global__ void __launch_bounds__(NT + 32) batch_bulk_kernel(const BatchDesc* __restrict__ desc, int nprob, int total,
+	const long long* __restrict__ step_base, int local, BulkLayout lay, int* err, long long wait)
+{
+	extern __shared__ __align__(128) unsigned char bk_smem[];
+	int* first = reinterpret_cast<int*>(bk_smem);
+	uint64_t* full = reinterpret_cast<uint64_t*>(bk_smem + tb_first_bytes(nprob));
+	uint64_t* done = full + kBulkNB;
+	volatile int* abort = reinterpret_cast<volatile int*>(reinterpret_cast<unsigned char*>(full) + kBulkBar - 8);
+	unsigned char* rings = reinterpret_cast<unsigned char*>(full);   // ring offsets count from here
+	for (int q = threadIdx.x; q < nprob; q += blockDim.x) first[q] = desc[q].first;
+	if (threadIdx.x == 0) {
+		for (int b = 0; b < kBulkNB; b++) {
+			mbar_init(&full[b], 1);
+			mbar_init(&done[b], NT / 32);
+		}
+		*abort = 0;
+		mbar_fence_init();
+	}
+	__syncthreads();
+	const bool producer = threadIdx.x >= NT;
+	if (producer && threadIdx.x != NT) return;
+	const long long step = *step_base + local;
+	uint32_t g = 0;
+	bool ok = true;
+	for (int item = blockIdx.x; item < total && ok; item += gridDim.x) {
+		int lo = 0, hi = nprob - 1;
+		while (lo < hi) {
+			const int mid = (lo + hi + 1) >> 1;
+			if (first[mid] <= item) lo = mid;
+			else hi = mid - 1;
+		}
+		const BatchDesc& d = desc[lo];
+		const int t = item - d.first;
+		Ptrs<S> p{};
+		batch_roles<S>(d, step, p);
+		const BulkRings& rg = lay.k[bulk_kind(d.stencil)];
+		switch (d.stencil) {
+		case KG_LAPLACIAN:
+			bulk_item<OpLaplacian<N>, N, S, NT, KC>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, d, t, p, rg, rings, full, done,
+				abort, g, producer, err, wait, ok);
+			break;
+		case KG_DIVERGENCE:
+			bulk_item<OpDivergence<N>, N, S, NT, KC>(OpDivergence<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, t, p, rg,
+				rings, full, done, abort, g, producer, err, wait, ok);
+			break;
+		case KG_WAVE13PT:
+			bulk_item<OpWave13pt<N>, N, S, NT, KC>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, t, p, rg, rings,
+				full, done, abort, g, producer, err, wait, ok);
+			break;
+		case KG_GAUSSBLUR:
+			bulk_item<OpGaussblur<N>, N, S, NT, KC>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]), N(d.c[3]),
+				N(d.c[4]), N(d.c[5]), N(d.c[6])}, d, t, p, rg, rings, full, done, abort, g, producer, err, wait, ok);
+			break;
+		default: break;
+		}
+	}
+	// the producer stays until the compute warps are done with the last step
+	if (producer && ok && g > 0) {
+		if (!mbar_wait(&done[(g - 1) % kBulkNB], ((g - 1) / kBulkNB) & 1, kTmaWaitCycles, abort)) {
+			atomicExch(err, 1);
+			for (uint32_t w = g > kBulkNB ? g - kBulkNB : 0; w < g; w++)
+				mbar_wait(&full[w % kBulkNB], (w / kBulkNB) & 1, kTmaWaitCycles);
 		}
 	}
 }

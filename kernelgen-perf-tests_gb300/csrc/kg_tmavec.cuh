@@ -137,14 +137,19 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 		for (int v = 0; v < V; v++)
 			if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid[r] |= 1u << v;
 	}
-	uint32_t g = 0;
+	// step counters kept incrementally: barrier index and phase of the step,
+	// and the ring slot of the step's plane of every input
+	int bi = 0;
+	uint32_t ph = 0;
 	ZRuns rz = runs;
 	int xr, yr, kb, nsteps;
 	while (rz.next(xr, yr, kb, nsteps)) {
+		int s0[6];
+#pragma unroll
+		for (int q = 0; q < G::NIN; q++) s0[q] = G::slot(q, kb);
+		const long long c0 = i0 + sy * j + sz * kb;
 		for (int s = 0; s < nsteps; s++) {
-			const int k = kb + s;
-			const uint32_t gs = g + s;
-			const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[gs % NB], (gs / NB) & 1, wait, abort));
+			const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[bi], ph, wait, abort));
 			if (!ok) {
 				if (lane == 0) {
 					*abort = 1;
@@ -156,13 +161,12 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 #pragma unroll
 			for (int q = 0; q < G::NIN; q++) {
 				const Halo h = Op::halo(q);
-				const int s0 = G::slot(q, k);
 #pragma unroll
 				for (int d = 0; d < ZS; d++)
 					if (d < G::NZ(q))
-						base[q][d] = sm + G::offset(q) + G::step_slot(q, s0, d - h.z0) * G::PS(q) + toff[q];
+						base[q][d] = sm + G::offset(q) + G::step_slot(q, s0[q], d - h.z0) * G::PS(q) + toff[q];
 			}
-			const long long c = i0 + sy * j + sz * k;
+			const long long c = c0 + sz * s;
 			S o[PY][3][V];
 			for_v<0, PY>([&](auto ri) {
 				constexpr int R = decltype(ri)::value;
@@ -177,15 +181,20 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 			});
 			// this warp is done with the step's planes
 			__syncwarp();
-			if (lane == 0) mbar_arrive(&done[gs % NB]);
+			if (lane == 0) mbar_arrive(&done[bi]);
 #pragma unroll
 			for (int r = 0; r < PY; r++)
 				if (valid[r]) {
 #pragma unroll
 					for (int q = 0; q < sl.nout; q++) vstore<S, V>(p.out[q] + c + r * RB * sy, o[r][q], valid[r]);
 				}
+			if (++bi == NB) {
+				bi = 0;
+				ph ^= 1;
+			}
+#pragma unroll
+			for (int q = 0; q < G::NIN; q++) s0[q] = G::step_slot(q, s0[q], 1);
 		}
-		g += nsteps;
 	}
 }
 
@@ -195,9 +204,12 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 #ifndef KG_TMAVEC_BUDGET
 #define KG_TMAVEC_BUDGET (100 * 1024)
 #endif
-// Rows of points per lane (each lane evaluates PY x V points per plane).
+// Rows of points per lane (each lane evaluates PY x V points per plane):
+// measured on GB300, two rows for 2-byte storage (BF16 wave13pt 720 -> 817
+// Gpts/s, uxx1 291 -> 334 at 1024x512x512) and one for FP32 (uxx1 279 ->
+// 242 with two; the others within 2 %).
 #ifndef KG_TMAVEC_PY
-#define KG_TMAVEC_PY 1
+#define KG_TMAVEC_PY 0
 #endif
 template <class Op, class S, int BX, int BY> struct TmaVecDepth {
 	template <int L> static constexpr int bytes() { return TGeo<Op, S, BX, BY, L>::total(); }
@@ -209,7 +221,8 @@ template <class Op, class S, int BX, int BY> struct TmaVecDepth {
 template <class Op, class N, class S>
 struct TmaVecLaunch {
 	static constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
-	static constexpr int V = 16 / (int)sizeof(S), NW = 8, PY = KG_TMAVEC_PY;
+	static constexpr int V = 16 / (int)sizeof(S), NW = 8;
+	static constexpr int PY = KG_TMAVEC_PY > 0 ? KG_TMAVEC_PY : (sizeof(S) == 2 ? 2 : 1);
 	static constexpr int BX = 128, BY = NW * (32 * V / BX) * PY;
 	static constexpr int L = TmaVecDepth<Op, S, BX, BY>::L;
 	static constexpr int kThreads = 32 * NW + 32;
