@@ -331,6 +331,10 @@ typedef struct {
 	int tiles;               /* tiles (blocks) of all problems per launch */
 	int nshapes;             /* configurations the tuner tries */
 	int temporal;            /* steps per launch (temporal-blocking factor) */
+	int staged;              /* 1: a tile of BX consecutive columns and KC
+	                            planes whose inputs are staged in shared
+	                            memory by bulk copies, one step per launch */
+	int reserved;
 	long long steps_done;
 } kg_batch_config;
 kg_status kg_batch_create(kg_batch* b, const kg_problem* probs, int nprob);

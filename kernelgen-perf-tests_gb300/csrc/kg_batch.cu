@@ -595,30 +595,36 @@ __device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>
 			long long fl, fh;
 			step_cols(s, fl, fh);
 			const int k = it.kb + s;
-			// planes of this step: the window at the first step, then the newest
+			// planes of this step: the window at the first step, then the
+			// newest; the byte count first, then the copies
 			unsigned bytes = 0;
-			BulkChunk<Op, S> ch[6][5];
-			int np[6], p0[6];
 #pragma unroll
 			for (int q = 0; q < NIN; q++) {
 				const Halo h = Op::halo(q);
-				p0[q] = k2d ? 0 : (s == 0 ? k - h.z0 : k + h.z1);
-				np[q] = k2d ? 1 : (s == 0 ? NZ(q) : 1);
-				for (int m = 0; m < np[q]; m++) {
-					ch[q][m].make(q, fl, fh, k2d ? 0 : (long long)(p0[q] + m) * it.P, it.nx, n);
-					bytes += (unsigned)ch[q][m].count * ES;
+				const int p0 = k2d ? 0 : (s == 0 ? k - h.z0 : k + h.z1);
+				const int np = k2d ? 1 : (s == 0 ? NZ(q) : 1);
+				for (int m = 0; m < np; m++) {
+					BulkChunk<Op, S> ch;
+					ch.make(q, fl, fh, k2d ? 0 : (long long)(p0 + m) * it.P, it.nx, n);
+					bytes += (unsigned)ch.count * ES;
 				}
 			}
 			mbar_expect_tx(&full[gs % kBulkNB], bytes);
 			fence_proxy_async();
 #pragma unroll
-			for (int q = 0; q < NIN; q++)
-				for (int m = 0; m < np[q]; m++) {
-					const int slot = (k2d ? s : p0[q] + m) % RZ(q);
-					if (ch[q][m].count > 0)
-						bulk_copy(sm + rg.off[q] + slot * rg.cap[q] * ES, p.in[q] + ch[q][m].st,
-							(unsigned)ch[q][m].count * ES, &full[gs % kBulkNB]);
+			for (int q = 0; q < NIN; q++) {
+				const Halo h = Op::halo(q);
+				const int p0 = k2d ? 0 : (s == 0 ? k - h.z0 : k + h.z1);
+				const int np = k2d ? 1 : (s == 0 ? NZ(q) : 1);
+				for (int m = 0; m < np; m++) {
+					BulkChunk<Op, S> ch;
+					ch.make(q, fl, fh, k2d ? 0 : (long long)(p0 + m) * it.P, it.nx, n);
+					const int slot = (k2d ? s : p0 + m) % RZ(q);
+					if (ch.count > 0)
+						bulk_copy(sm + rg.off[q] + slot * rg.cap[q] * ES, p.in[q] + ch.st, (unsigned)ch.count * ES,
+							&full[gs % kBulkNB]);
 				}
+			}
 			issued = gs + 1;
 		}
 		if (!ok) {
@@ -779,7 +785,15 @@ static const int k_nshapes = sizeof(k_shapes) / sizeof(k_shapes[0]);
 static const TBShape k_tb_shapes[] = {{32, 8, 8, 2}, {32, 8, 4, 2}, {32, 4, 4, 2}, {64, 4, 4, 2}, {64, 8, 4, 2},
 	{32, 8, 8, 3}, {32, 4, 4, 3}, {64, 4, 4, 3}, {32, 8, 8, 4}, {32, 4, 4, 4}};
 static const int k_ntb = sizeof(k_tb_shapes) / sizeof(k_tb_shapes[0]);
-static const int k_nconfigs = k_nshapes + k_ntb;
+// Bulk-staged one-step tiles (NT consecutive columns, KC planes); configuration
+// index k_nshapes + k_ntb + i.
+struct BulkShape { int nt, kc; };
+static const BulkShape k_bulk_shapes[] = {{256, 16}, {256, 8}, {256, 32}, {128, 16}, {128, 32}};
+static const int k_nbulk = sizeof(k_bulk_shapes) / sizeof(k_bulk_shapes[0]);
+static const int k_bulk0 = k_nshapes + k_ntb;
+static const int k_nconfigs = k_nshapes + k_ntb + k_nbulk;
+static bool is_temporal(int shape) { return shape >= k_nshapes && shape < k_bulk0; }
+static bool is_bulk(int shape) { return shape >= k_bulk0; }
 // Steps each tuning trial times (a multiple of every temporal factor).
 constexpr int kTuneSteps = 12;
 constexpr int kSmemOptin = 227 * 1024;
@@ -899,6 +913,105 @@ static int tb_occupancy(size_t smem)
 	return n;
 }
 
+// Ring layout of the bulk kernel for these problems: per stencil kind and
+// input, a slot holds the largest plane range any of its problems copies
+// (the NT columns' span, grown by the input's reach, plus 16-byte rounding at
+// both ends); NZ + kBulkL slots per input.  Returns the dynamic shared memory
+// (first-tile table, mbarriers, rings), 0 if an array is not 16-byte aligned
+// or a problem has 2^31 points or more.
+template <class Op> static void bulk_rings_of(const kg_problem& p, int nt, int es, BulkRings& r, int& bytes)
+{
+	constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
+	constexpr Slots sl = Op::slots();
+	const int A = 16 / es;
+	const long long dxn = std::max(1, p.nx - Op::LX - Op::HX);
+	const long long span = (nt - 1) + ((nt - 1) / dxn + 1) * (Op::LX + Op::HX);
+	int off = bytes;
+	for (int q = 0; q < sl.nin; q++) {
+		const Halo h = Op::halo(q);
+		const long long need = span + h.x0 + h.x1 + (long long)(h.y0 + h.y1) * p.nx + 1 + 2 * (A - 1);
+		const int cap = (int)((need + A - 1) / A * A);
+		r.cap[q] = std::max(r.cap[q], cap);
+	}
+	for (int q = 0; q < sl.nin; q++) {
+		const int nz = k2d ? 1 : Op::halo(q).z0 + Op::halo(q).z1 + 1;
+		r.off[q] = off;
+		off += (nz + kBulkL) * r.cap[q] * es;
+	}
+	bytes = off;
+}
+
+static size_t bulk_layout(const std::vector<kg_problem>& probs, int es, int nt, BulkLayout* lay)
+{
+	memset(lay, 0, sizeof(*lay));
+	int bytes[4] = {kBulkBar, kBulkBar, kBulkBar, kBulkBar};
+	for (const kg_problem& p : probs) {
+		const long long n = (long long)p.nx * p.ny * p.ns;
+		if (n >= (1LL << 31)) return 0;
+		for (int k = 0; k < kg_stencil_narrays(p.stencil); k++)
+			if ((uintptr_t)p.arr[k] % 16) return 0;
+	}
+	// caps first (maximum over the problems of a kind), then offsets
+	for (int pass = 0; pass < 2; pass++)
+		for (const kg_problem& p : probs) {
+			const int k = bulk_kind(p.stencil);
+			int b = kBulkBar;
+			switch (p.stencil) {
+			case KG_LAPLACIAN: bulk_rings_of<OpLaplacian<FF>>(p, nt, es, lay->k[k], b); break;
+			case KG_DIVERGENCE: bulk_rings_of<OpDivergence<FF>>(p, nt, es, lay->k[k], b); break;
+			case KG_WAVE13PT: bulk_rings_of<OpWave13pt<FF>>(p, nt, es, lay->k[k], b); break;
+			case KG_GAUSSBLUR: bulk_rings_of<OpGaussblur<FF>>(p, nt, es, lay->k[k], b); break;
+			default: break;
+			}
+			bytes[k] = std::max(bytes[k], b);
+		}
+	const int m = std::max(std::max(bytes[0], bytes[1]), std::max(bytes[2], bytes[3]));
+	return (size_t)tb_first_bytes((int)probs.size()) + (size_t)m;
+}
+
+template <class N, class S, int NT, int KC>
+static int bulk_occ(size_t smem)
+{
+	static std::atomic<bool> set[64];   // the shared-memory opt-in, once per device
+	int dev = 0;
+	cudaGetDevice(&dev);
+	if (dev >= 0 && dev < 64 && !set[dev].load(std::memory_order_acquire)) {
+		cudaFuncSetAttribute(batch_bulk_kernel<N, S, NT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptin);
+		set[dev].store(true, std::memory_order_release);
+	}
+	int n = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_bulk_kernel<N, S, NT, KC>, NT + 32, smem);
+	return n;
+}
+
+template <class N, class S>
+static int bulk_occupancy(int i, size_t smem)
+{
+	switch (i) {
+	case 0: return bulk_occ<N, S, 256, 16>(smem);
+	case 1: return bulk_occ<N, S, 256, 8>(smem);
+	case 2: return bulk_occ<N, S, 256, 32>(smem);
+	case 3: return bulk_occ<N, S, 128, 16>(smem);
+	case 4: return bulk_occ<N, S, 128, 32>(smem);
+	default: return 0;
+	}
+}
+
+template <class N, class S>
+static cudaError_t bulk_launch(int i, dim3 grid, size_t smem, const BatchDesc* desc, int nprob, int total,
+	const long long* base, int local, const BulkLayout& lay, int* err, long long wait, cudaStream_t st)
+{
+	switch (i) {
+	case 0: batch_bulk_kernel<N, S, 256, 16><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 1: batch_bulk_kernel<N, S, 256, 8><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 2: batch_bulk_kernel<N, S, 256, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 3: batch_bulk_kernel<N, S, 128, 16><<<grid, 128 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 4: batch_bulk_kernel<N, S, 128, 32><<<grid, 128 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	default: return cudaErrorInvalidValue;
+	}
+	return cudaGetLastError();
+}
+
 }  // namespace kg
 
 using namespace kg;
@@ -917,6 +1030,8 @@ struct kg_batch_s {
 	int graph_steps = 0;
 	void* scratch = nullptr;       // temporal tiles: the second set of the rotating arrays
 	size_t tb_smem = 0;            // temporal tiles: dynamic shared memory of a launch
+	size_t bulk_smem = 0;          // bulk-staged tiles: dynamic shared memory, ring layout
+	BulkLayout bulk_lay;
 };
 
 static int es_of(const kg_batch_s* b) { return b->dtype == KG_F32 ? 4 : 8; }
@@ -950,9 +1065,21 @@ static kg_status batch_build_table(kg_batch_s* b, int shape)
 {
 	std::vector<BatchDesc> h(b->probs.size());
 	int first = 0;
-	const bool temporal = shape >= k_nshapes;
+	const bool temporal = is_temporal(shape);
 	std::vector<void*> sets;
 	size_t next = 0;
+	if (is_bulk(shape)) {
+		const int i = shape - k_bulk0;
+		const size_t smem = bulk_layout(b->probs, es_of(b), k_bulk_shapes[i].nt, &b->bulk_lay);
+		if (smem == 0)
+			return fail(KG_EINVAL, "kg_batch: the bulk-staged tiles need 16-byte aligned arrays of fewer than 2^31 points");
+		if (smem > (size_t)kSmemOptin)
+			return fail(KG_EINVAL, "kg_batch: bulk shape %d needs %zu bytes of shared memory for these problems",
+				shape, smem);
+		const int occ = b->dtype == KG_F32 ? bulk_occupancy<FF, float>(i, smem) : bulk_occupancy<SD, double>(i, smem);
+		if (occ < 1) return fail(KG_EINVAL, "kg_batch: bulk shape %d does not fit an SM", shape);
+		b->bulk_smem = smem;
+	}
 	if (temporal) {
 		const TBShape& sh = k_tb_shapes[shape - k_nshapes];
 		const size_t smem = tb_smem_bytes(b->probs, es_of(b), sh, sh.t);
@@ -985,6 +1112,9 @@ static kg_status batch_build_table(kg_batch_s* b, int shape)
 			if (t > 0x7fffffffLL) return fail(KG_EINVAL, "kg_batch: more than 2^31 tiles");
 			d.tiles_x = (int)t;
 			d.tiles_y = d.tiles_z = 1;
+		} else if (is_bulk(shape)) {
+			const BulkShape& bs = k_bulk_shapes[shape - k_bulk0];
+			tiles_of(p.stencil, p.nx, p.ny, p.ns, Shape{bs.nt, 1, bs.kc}, &d.tiles_x, &d.tiles_y, &d.tiles_z);
 		} else {
 			tiles_of(p.stencil, p.nx, p.ny, p.ns, k_shapes[shape], &d.tiles_x, &d.tiles_y, &d.tiles_z);
 		}
@@ -1030,7 +1160,21 @@ static cudaError_t batch_launch_steps(kg_batch_s* b, int nsteps, cudaStream_t st
 {
 	const dim3 grid(b->sms * b->ctas);
 	const int np = (int)b->probs.size();
-	if (b->shape >= k_nshapes) {
+	if (is_bulk(b->shape)) {
+		int* err = tma_error_flag();
+		if (!err) return cudaErrorInvalidSymbol;
+		const long long wait = tma_wait_limit();
+		const int i = b->shape - k_bulk0;
+		for (int s = 0; s < nsteps; s++) {
+			cudaError_t e = (b->dtype == KG_F32)
+				? bulk_launch<FF, float>(i, grid, b->bulk_smem, b->d_desc, np, b->total, b->d_step, s, b->bulk_lay, err, wait, st)
+				: bulk_launch<SD, double>(i, grid, b->bulk_smem, b->d_desc, np, b->total, b->d_step, s, b->bulk_lay, err, wait, st);
+			if (e != cudaSuccess) return e;
+		}
+		batch_advance<<<1, 32, 0, st>>>(b->d_step, nsteps);
+		return cudaGetLastError();
+	}
+	if (is_temporal(b->shape)) {
 		cudaError_t e = b->dtype == KG_F32 ? batch_tb_steps<FF, float>(b, nsteps, st)
 		                                   : batch_tb_steps<SD, double>(b, nsteps, st);
 		if (e != cudaSuccess) return e;
@@ -1131,7 +1275,15 @@ kg_status kg_batch_get_config(kg_batch b, kg_batch_config* cfg)
 	clear_error();
 	if (!b || !cfg) return fail(KG_EINVAL, "kg_batch_get_config: bad argument");
 	cfg->shape = b->shape;
-	if (b->shape >= k_nshapes) {
+	cfg->staged = 0;
+	if (is_bulk(b->shape)) {
+		const BulkShape& bs = k_bulk_shapes[b->shape - k_bulk0];
+		cfg->bx = bs.nt;
+		cfg->by = 1;
+		cfg->kc = bs.kc;
+		cfg->temporal = 1;
+		cfg->staged = 1;
+	} else if (is_temporal(b->shape)) {
 		const TBShape& t = k_tb_shapes[b->shape - k_nshapes];
 		cfg->bx = t.bx;
 		cfg->by = t.by;
@@ -1229,6 +1381,13 @@ kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream)
 		int occ;
 		if (sh < k_nshapes) {
 			occ = b->dtype == KG_F32 ? shape_occupancy<FF, float>(sh) : shape_occupancy<SD, double>(sh);
+		} else if (is_bulk(sh)) {
+			BulkLayout lay;
+			const size_t smem = bulk_layout(b->probs, es_of(b), k_bulk_shapes[sh - k_bulk0].nt, &lay);
+			if (smem == 0 || smem > (size_t)kSmemOptin) continue;
+			occ = b->dtype == KG_F32 ? bulk_occupancy<FF, float>(sh - k_bulk0, smem)
+			                         : bulk_occupancy<SD, double>(sh - k_bulk0, smem);
+			if (occ < 1) continue;
 		} else {
 			const TBShape& t = k_tb_shapes[sh - k_nshapes];
 			const size_t smem = tb_smem_bytes(b->probs, es_of(b), t, t.t);

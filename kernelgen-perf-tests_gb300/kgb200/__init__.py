@@ -71,7 +71,8 @@ class KgPeaks(ctypes.Structure):
 class KgBatchConfig(ctypes.Structure):
     _fields_ = [("shape", ctypes.c_int), ("bx", ctypes.c_int), ("by", ctypes.c_int), ("kc", ctypes.c_int),
                 ("ctas_per_sm", ctypes.c_int), ("tiles", ctypes.c_int), ("nshapes", ctypes.c_int),
-                ("temporal", ctypes.c_int), ("steps_done", ctypes.c_longlong)]
+                ("temporal", ctypes.c_int), ("staged", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("steps_done", ctypes.c_longlong)]
 
 
 class KgSolveOpts(ctypes.Structure):

@@ -173,6 +173,53 @@ def test_batch_temporal_blocks_equal_individual_sweeps(dtype):
     b.close()
 
 
+def bulk_configs(b):
+    """Configuration indices of the bulk-staged tiles."""
+    out = []
+    for shape in range(b.config().nshapes):
+        try:
+            b.set_config(shape, 2)
+        except kgb200.KgError:
+            continue
+        if b.config().staged:
+            out.append(shape)
+    return out
+
+
+@pytest.mark.parametrize("dtype", [kgb200.KG_F32, kgb200.KG_F64])
+def test_batch_bulk_tiles_equal_individual_sweeps(dtype):
+    """The tiles whose inputs are staged in shared memory by bulk copies, in
+    every shape, on problems whose sizes leave arrays that end off a 16-byte
+    boundary (their last range is read from global memory), plain steps and
+    graph replays: every array equals the problem's own kg_sweep calls."""
+    n = 40
+    probs, bufs, meta = make_batch(n, dtype, seed=23, lo=5, hi=70)
+    saved = [[a.clone() for a in arrs] for arrs in bufs]
+    ref = reference_run(meta, bufs, dtype, 7)
+    b = kgb200.Batch(probs)
+    configs = bulk_configs(b)
+    assert configs, "no bulk configuration is available"
+    for shape in configs:
+        for q in range(n):
+            for a, s in zip(bufs[q], saved[q]):
+                a.copy_(s)
+        b.set_config(shape, 1 + shape % 4)
+        b.set_step(0)
+        b.step(3)
+        b.capture(2)
+        b.launch()
+        b.launch()
+        torch.cuda.synchronize()
+        kgb200.engine_status()
+        assert b.config().steps_done == 7
+        got = batch_final(b, bufs, n)
+        for q in range(n):
+            for k, (g, w) in enumerate(zip(got[q], ref[q])):
+                assert torch.equal(g, w), "config %d problem %d (%s %s) array %d differs" % (
+                    shape, q, meta[q][0], meta[q][1], k)
+    b.close()
+
+
 def test_batch_f64_matches_oracle():
     probs, bufs, meta = make_batch(6, kgb200.KG_F64, seed=21)
     host = [[a.cpu().numpy().copy() for a in arrs] for arrs in bufs]
