@@ -509,13 +509,15 @@ __device__ __forceinline__ void bulk_copy(void* dst_smem, const void* src, unsig
 		::"r"(smem_addr(dst_smem)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 
-// One item (tile) of the batch as the bulk kernel walks it.
+// One item (tile) of the batch as the bulk kernel walks it: NC = NT CPT
+// consecutive interior columns per step (each thread takes CPT of them, NT
+// apart); 3D: the same columns on KC planes; 2D: KC groups of NC columns.
 template <class Op> struct BulkItem {
 	static constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
 	int nx, ny, ns, dxn;
 	long long ncol, col0, P;
 	int kb, nsteps;
-	__device__ __forceinline__ void init(const BatchDesc& d, int t, int NT, int KC) {
+	__device__ __forceinline__ void init(const BatchDesc& d, int t, int NC, int KC) {
 		nx = d.nx;
 		ny = d.ny;
 		ns = d.ns;
@@ -524,11 +526,11 @@ template <class Op> struct BulkItem {
 		P = (long long)nx * ny;
 		const int tcol = t % d.tiles_x, tz = t / d.tiles_x;
 		if (k2d) {
-			col0 = (long long)tcol * KC * NT;
+			col0 = (long long)tcol * KC * NC;
 			kb = 0;
-			nsteps = (int)min((long long)KC, (ncol - col0 + NT - 1) / NT);
+			nsteps = (int)min((long long)KC, (ncol - col0 + NC - 1) / NC);
 		} else {
-			col0 = (long long)tcol * NT;
+			col0 = (long long)tcol * NC;
 			kb = Op::LZ + tz * KC;
 			nsteps = min(KC, ns - Op::HZ - kb);
 		}
@@ -562,7 +564,7 @@ template <class Op, class S> struct BulkChunk {
 	}
 };
 
-template <class Op, class N, class S, int NT, int KC>
+template <class Op, class N, class S, int NT, int CPT, int KC>
 __device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>& p, const BulkRings& rg,
 	unsigned char* sm, uint64_t* full, uint64_t* done, volatile int* abort, uint32_t& g, bool producer, int* err,
 	long long wait, bool& ok)
@@ -571,15 +573,17 @@ __device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>
 	constexpr Slots sl = Op::slots();
 	constexpr int NIN = sl.nin;
 	constexpr int ES = (int)sizeof(S);
+	constexpr int A = 16 / ES;
+	constexpr int NC = NT * CPT;
 	BulkItem<Op> it;
-	it.init(d, t, NT, KC);
+	it.init(d, t, NC, KC);
 	const long long n = it.P * it.ns;
 	auto NZ = [](int q) { return k2d ? 1 : Op::halo(q).z0 + Op::halo(q).z1 + 1; };
-	auto RZ = [&](int q) { return NZ(q) + kBulkL; };
-	// the range of step s: columns and plane
+	auto RZ = [](int q) { return (k2d ? 1 : Op::halo(q).z0 + Op::halo(q).z1 + 1) + kBulkL; };
+	// the columns of step s: first and last full index
 	auto step_cols = [&](int s, long long& fl, long long& fh) {
-		const long long c0 = k2d ? it.col0 + (long long)s * NT : it.col0;
-		const long long c1 = min(c0 + NT, it.ncol) - 1;
+		const long long c0 = k2d ? it.col0 + (long long)s * NC : it.col0;
+		const long long c1 = min(c0 + NC, it.ncol) - 1;
 		fl = it.f(c0);
 		fh = it.f(c1);
 	};
@@ -639,6 +643,29 @@ __device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>
 	}
 	// ---- compute warps ----
 	const int tid = threadIdx.x, lane = tid & 31;
+	// 3D: the columns, their full indices and the chunks' placement are the
+	// same on every plane of the item; whether an input's chunk reaches past
+	// the array's last whole 16 bytes is checked on the item's last window
+	long long fl = 0, fh = 0;
+	long long fc[CPT];
+	bool cv[CPT];
+	bool item_cut = false;
+	if (!k2d) {
+		step_cols(0, fl, fh);
+#pragma unroll
+		for (int r = 0; r < CPT; r++) {
+			const long long col = it.col0 + tid + r * NT;
+			cv[r] = col < it.ncol;
+			fc[r] = it.f(cv[r] ? col : it.col0);
+		}
+#pragma unroll
+		for (int q = 0; q < NIN; q++) {
+			BulkChunk<Op, S> ch;
+			ch.make(q, fl, fh, (long long)(it.kb + it.nsteps - 1 + Op::halo(q).z1) * it.P, it.nx, n);
+			item_cut = item_cut || ch.cut;
+		}
+	}
+	const int pm = (int)(it.P & (A - 1));
 	for (int s = 0; s < it.nsteps; s++) {
 		const uint32_t gs = g + s;
 		const bool got = __all_sync(0xffffffffu, mbar_wait(&full[gs % kBulkNB], (gs / kBulkNB) & 1, wait, abort));
@@ -650,59 +677,80 @@ __device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>
 			ok = false;
 			return;
 		}
-		long long fl, fh;
-		step_cols(s, fl, fh);
-		const long long c0 = k2d ? it.col0 + (long long)s * NT : it.col0;
-		const long long col = c0 + tid;
 		const int k = it.kb + s;
-		if (col < it.ncol) {
-			const long long fc = it.f(col);
-			const long long pk = k2d ? 0 : (long long)k * it.P;
-			bool cut = false;
-			// byte address of the point's own element in each (input, plane) slot
-			const unsigned char* a[6][5];
+		bool cut = item_cut;
+		if (k2d) {
+			step_cols(s, fl, fh);
+			const long long c0 = it.col0 + (long long)s * NC;
+#pragma unroll
+			for (int r = 0; r < CPT; r++) {
+				const long long col = c0 + tid + r * NT;
+				cv[r] = col < it.ncol;
+				fc[r] = it.f(cv[r] ? col : c0);
+			}
+#pragma unroll
+			for (int q = 0; q < NIN; q++) {
+				BulkChunk<Op, S> ch;
+				ch.make(q, fl, fh, 0, it.nx, n);
+				cut = cut || ch.cut;
+			}
+		}
+		const long long pk = k2d ? 0 : (long long)k * it.P;
+		N o[CPT][3];
+		if (!cut) {
+			// per (input, plane): the byte offset, from the rings' base, that
+			// full index 0 of the chunk's plane would have, so that element fc
+			// lies at byte b + fc ES
+			long long b[6][5];
 #pragma unroll
 			for (int q = 0; q < NIN; q++) {
 				const Halo h = Op::halo(q);
+				const long long lob = fl - (h.x0 + (long long)h.y0 * it.nx);   // first needed index, plane-relative
 #pragma unroll
 				for (int m = 0; m < 5; m++) {
 					if (m >= NZ(q)) continue;
 					const int pl = k2d ? 0 : k - h.z0 + m;
-					BulkChunk<Op, S> ch;
-					ch.make(q, fl, fh, k2d ? 0 : (long long)pl * it.P, it.nx, n);
-					cut = cut || ch.cut;
+					const int phase = (int)((lob + (long long)pl * pm) & (A - 1));
 					const int slot = (k2d ? s : pl) % RZ(q);
-					const long long rel = fc - fl + (h.x0 + (long long)h.y0 * it.nx) + ch.phase;
-					a[q][m] = sm + rg.off[q] + slot * rg.cap[q] * ES + rel * ES;
+					b[q][m] = rg.off[q] + (long long)slot * rg.cap[q] * ES + (phase - lob) * ES;
 				}
 			}
-			N o[3];
-			if (!cut) {
+#pragma unroll
+			for (int r = 0; r < CPT; r++) {
 				struct Acc {
-					const unsigned char* (*a)[5];
+					const unsigned char* sm;
+					long long (*b)[5];
+					long long fc;
 					int nx;
 					__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
-						return Conv<N, S>::from(*reinterpret_cast<const S*>(a[q][dz + Op::halo(q).z0] + (dx + dy * nx) * ES));
+						return Conv<N, S>::from(raw(q, dx, dy, dz));
 					}
 					__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
-						return *reinterpret_cast<const S*>(a[q][dz + Op::halo(q).z0] + (dx + dy * nx) * ES);
+						return *reinterpret_cast<const S*>(sm + (b[q][dz + Op::halo(q).z0] + (fc + dx + dy * nx) * ES));
 					}
-				} at{a, it.nx};
-				op.point(at, o);
-			} else {
-				GAcc<N, S> at{p.in, fc + pk, it.nx, it.P};
-				op.point(at, o);
+				} at{sm, b, fc[r], it.nx};
+				op.point(at, o[r]);
 			}
+		} else {
 #pragma unroll
-			for (int q = 0; q < sl.nout; q++) p.out[q][fc + pk] = Conv<N, S>::to(o[q]);
+			for (int r = 0; r < CPT; r++) {
+				GAcc<N, S> at{p.in, fc[r] + pk, it.nx, it.P};
+				op.point(at, o[r]);
+			}
 		}
+		// the step's inputs are read: this warp is done with its planes
 		__syncwarp();
 		if (lane == 0) mbar_arrive(&done[gs % kBulkNB]);
+#pragma unroll
+		for (int r = 0; r < CPT; r++)
+			if (cv[r])
+#pragma unroll
+				for (int q = 0; q < sl.nout; q++) p.out[q][fc[r] + pk] = Conv<N, S>::to(o[r][q]);
 	}
 	g += it.nsteps;
 }
 
-template <class N, class S, int NT, int KC>
+template <class N, class S, int NT, int CPT, int KC>
 __global__ void __launch_bounds__(NT + 32) batch_bulk_kernel(const BatchDesc* __restrict__ desc, int nprob, int total,
 	const long long* __restrict__ step_base, int local, BulkLayout lay, int* err, long long wait)
 {
@@ -741,19 +789,19 @@ __global__ void __launch_bounds__(NT + 32) batch_bulk_kernel(const BatchDesc* __
 		const BulkRings& rg = lay.k[bulk_kind(d.stencil)];
 		switch (d.stencil) {
 		case KG_LAPLACIAN:
-			bulk_item<OpLaplacian<N>, N, S, NT, KC>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, d, t, p, rg, rings, full, done,
+			bulk_item<OpLaplacian<N>, N, S, NT, CPT, KC>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, d, t, p, rg, rings, full, done,
 				abort, g, producer, err, wait, ok);
 			break;
 		case KG_DIVERGENCE:
-			bulk_item<OpDivergence<N>, N, S, NT, KC>(OpDivergence<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, t, p, rg,
+			bulk_item<OpDivergence<N>, N, S, NT, CPT, KC>(OpDivergence<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, t, p, rg,
 				rings, full, done, abort, g, producer, err, wait, ok);
 			break;
 		case KG_WAVE13PT:
-			bulk_item<OpWave13pt<N>, N, S, NT, KC>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, t, p, rg, rings,
+			bulk_item<OpWave13pt<N>, N, S, NT, CPT, KC>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, t, p, rg, rings,
 				full, done, abort, g, producer, err, wait, ok);
 			break;
 		case KG_GAUSSBLUR:
-			bulk_item<OpGaussblur<N>, N, S, NT, KC>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]), N(d.c[3]),
+			bulk_item<OpGaussblur<N>, N, S, NT, CPT, KC>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]), N(d.c[3]),
 				N(d.c[4]), N(d.c[5]), N(d.c[6])}, d, t, p, rg, rings, full, done, abort, g, producer, err, wait, ok);
 			break;
 		default: break;
@@ -787,8 +835,8 @@ static const TBShape k_tb_shapes[] = {{32, 8, 8, 2}, {32, 8, 4, 2}, {32, 4, 4, 2
 static const int k_ntb = sizeof(k_tb_shapes) / sizeof(k_tb_shapes[0]);
 // Bulk-staged one-step tiles (NT consecutive columns, KC planes); configuration
 // index k_nshapes + k_ntb + i.
-struct BulkShape { int nt, kc; };
-static const BulkShape k_bulk_shapes[] = {{256, 16}, {256, 8}, {256, 32}, {128, 16}, {128, 32}};
+struct BulkShape { int nt, cpt, kc; };
+static const BulkShape k_bulk_shapes[] = {{256, 4, 16}, {256, 2, 16}, {256, 4, 32}, {128, 4, 32}, {256, 1, 32}};
 static const int k_nbulk = sizeof(k_bulk_shapes) / sizeof(k_bulk_shapes[0]);
 static const int k_bulk0 = k_nshapes + k_ntb;
 static const int k_nconfigs = k_nshapes + k_ntb + k_nbulk;
@@ -969,18 +1017,18 @@ static size_t bulk_layout(const std::vector<kg_problem>& probs, int es, int nt, 
 	return (size_t)tb_first_bytes((int)probs.size()) + (size_t)m;
 }
 
-template <class N, class S, int NT, int KC>
+template <class N, class S, int NT, int CPT, int KC>
 static int bulk_occ(size_t smem)
 {
 	static std::atomic<bool> set[64];   // the shared-memory opt-in, once per device
 	int dev = 0;
 	cudaGetDevice(&dev);
 	if (dev >= 0 && dev < 64 && !set[dev].load(std::memory_order_acquire)) {
-		cudaFuncSetAttribute(batch_bulk_kernel<N, S, NT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptin);
+		cudaFuncSetAttribute(batch_bulk_kernel<N, S, NT, CPT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptin);
 		set[dev].store(true, std::memory_order_release);
 	}
 	int n = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_bulk_kernel<N, S, NT, KC>, NT + 32, smem);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_bulk_kernel<N, S, NT, CPT, KC>, NT + 32, smem);
 	return n;
 }
 
@@ -988,11 +1036,11 @@ template <class N, class S>
 static int bulk_occupancy(int i, size_t smem)
 {
 	switch (i) {
-	case 0: return bulk_occ<N, S, 256, 16>(smem);
-	case 1: return bulk_occ<N, S, 256, 8>(smem);
-	case 2: return bulk_occ<N, S, 256, 32>(smem);
-	case 3: return bulk_occ<N, S, 128, 16>(smem);
-	case 4: return bulk_occ<N, S, 128, 32>(smem);
+	case 0: return bulk_occ<N, S, 256, 4, 16>(smem);
+	case 1: return bulk_occ<N, S, 256, 2, 16>(smem);
+	case 2: return bulk_occ<N, S, 256, 4, 32>(smem);
+	case 3: return bulk_occ<N, S, 128, 4, 32>(smem);
+	case 4: return bulk_occ<N, S, 256, 1, 32>(smem);
 	default: return 0;
 	}
 }
@@ -1002,11 +1050,11 @@ static cudaError_t bulk_launch(int i, dim3 grid, size_t smem, const BatchDesc* d
 	const long long* base, int local, const BulkLayout& lay, int* err, long long wait, cudaStream_t st)
 {
 	switch (i) {
-	case 0: batch_bulk_kernel<N, S, 256, 16><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 1: batch_bulk_kernel<N, S, 256, 8><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 2: batch_bulk_kernel<N, S, 256, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 3: batch_bulk_kernel<N, S, 128, 16><<<grid, 128 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 4: batch_bulk_kernel<N, S, 128, 32><<<grid, 128 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 0: batch_bulk_kernel<N, S, 256, 4, 16><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 1: batch_bulk_kernel<N, S, 256, 2, 16><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 2: batch_bulk_kernel<N, S, 256, 4, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 3: batch_bulk_kernel<N, S, 128, 4, 32><<<grid, 128 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 4: batch_bulk_kernel<N, S, 256, 1, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
 	default: return cudaErrorInvalidValue;
 	}
 	return cudaGetLastError();
@@ -1070,7 +1118,7 @@ static kg_status batch_build_table(kg_batch_s* b, int shape)
 	size_t next = 0;
 	if (is_bulk(shape)) {
 		const int i = shape - k_bulk0;
-		const size_t smem = bulk_layout(b->probs, es_of(b), k_bulk_shapes[i].nt, &b->bulk_lay);
+		const size_t smem = bulk_layout(b->probs, es_of(b), k_bulk_shapes[i].nt * k_bulk_shapes[i].cpt, &b->bulk_lay);
 		if (smem == 0)
 			return fail(KG_EINVAL, "kg_batch: the bulk-staged tiles need 16-byte aligned arrays of fewer than 2^31 points");
 		if (smem > (size_t)kSmemOptin)
@@ -1114,7 +1162,7 @@ static kg_status batch_build_table(kg_batch_s* b, int shape)
 			d.tiles_y = d.tiles_z = 1;
 		} else if (is_bulk(shape)) {
 			const BulkShape& bs = k_bulk_shapes[shape - k_bulk0];
-			tiles_of(p.stencil, p.nx, p.ny, p.ns, Shape{bs.nt, 1, bs.kc}, &d.tiles_x, &d.tiles_y, &d.tiles_z);
+			tiles_of(p.stencil, p.nx, p.ny, p.ns, Shape{bs.nt * bs.cpt, 1, bs.kc}, &d.tiles_x, &d.tiles_y, &d.tiles_z);
 		} else {
 			tiles_of(p.stencil, p.nx, p.ny, p.ns, k_shapes[shape], &d.tiles_x, &d.tiles_y, &d.tiles_z);
 		}
@@ -1279,7 +1327,7 @@ kg_status kg_batch_get_config(kg_batch b, kg_batch_config* cfg)
 	if (is_bulk(b->shape)) {
 		const BulkShape& bs = k_bulk_shapes[b->shape - k_bulk0];
 		cfg->bx = bs.nt;
-		cfg->by = 1;
+		cfg->by = bs.cpt;
 		cfg->kc = bs.kc;
 		cfg->temporal = 1;
 		cfg->staged = 1;
@@ -1383,7 +1431,7 @@ kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream)
 			occ = b->dtype == KG_F32 ? shape_occupancy<FF, float>(sh) : shape_occupancy<SD, double>(sh);
 		} else if (is_bulk(sh)) {
 			BulkLayout lay;
-			const size_t smem = bulk_layout(b->probs, es_of(b), k_bulk_shapes[sh - k_bulk0].nt, &lay);
+			const size_t smem = bulk_layout(b->probs, es_of(b), k_bulk_shapes[sh - k_bulk0].nt * k_bulk_shapes[sh - k_bulk0].cpt, &lay);
 			if (smem == 0 || smem > (size_t)kSmemOptin) continue;
 			occ = b->dtype == KG_F32 ? bulk_occupancy<FF, float>(sh - k_bulk0, smem)
 			                         : bulk_occupancy<SD, double>(sh - k_bulk0, smem);
