@@ -750,8 +750,9 @@ __device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>
 	g += it.nsteps;
 }
 
+// Registers bounded for three CTAs of 256 compute threads per SM.
 template <class N, class S, int NT, int CPT, int KC>
-__global__ void __launch_bounds__(NT + 32) batch_bulk_kernel(const BatchDesc* __restrict__ desc, int nprob, int total,
+__global__ void __launch_bounds__(NT + 32, 768 / NT) batch_bulk_kernel(const BatchDesc* __restrict__ desc, int nprob, int total,
 	const long long* __restrict__ step_base, int local, BulkLayout lay, int* err, long long wait)
 {
 	extern __shared__ __align__(128) unsigned char bk_smem[];
@@ -836,7 +837,7 @@ static const int k_ntb = sizeof(k_tb_shapes) / sizeof(k_tb_shapes[0]);
 // Bulk-staged one-step tiles (NT consecutive columns, KC planes); configuration
 // index k_nshapes + k_ntb + i.
 struct BulkShape { int nt, cpt, kc; };
-static const BulkShape k_bulk_shapes[] = {{256, 4, 16}, {256, 2, 16}, {256, 4, 32}, {128, 4, 32}, {256, 1, 32}};
+static const BulkShape k_bulk_shapes[] = {{256, 4, 32}, {256, 8, 32}, {256, 4, 64}, {512, 2, 32}, {128, 8, 32}};
 static const int k_nbulk = sizeof(k_bulk_shapes) / sizeof(k_bulk_shapes[0]);
 static const int k_bulk0 = k_nshapes + k_ntb;
 static const int k_nconfigs = k_nshapes + k_ntb + k_nbulk;
@@ -1036,11 +1037,11 @@ template <class N, class S>
 static int bulk_occupancy(int i, size_t smem)
 {
 	switch (i) {
-	case 0: return bulk_occ<N, S, 256, 4, 16>(smem);
-	case 1: return bulk_occ<N, S, 256, 2, 16>(smem);
-	case 2: return bulk_occ<N, S, 256, 4, 32>(smem);
-	case 3: return bulk_occ<N, S, 128, 4, 32>(smem);
-	case 4: return bulk_occ<N, S, 256, 1, 32>(smem);
+	case 0: return bulk_occ<N, S, 256, 4, 32>(smem);
+	case 1: return bulk_occ<N, S, 256, 8, 32>(smem);
+	case 2: return bulk_occ<N, S, 256, 4, 64>(smem);
+	case 3: return bulk_occ<N, S, 512, 2, 32>(smem);
+	case 4: return bulk_occ<N, S, 128, 8, 32>(smem);
 	default: return 0;
 	}
 }
@@ -1050,11 +1051,11 @@ static cudaError_t bulk_launch(int i, dim3 grid, size_t smem, const BatchDesc* d
 	const long long* base, int local, const BulkLayout& lay, int* err, long long wait, cudaStream_t st)
 {
 	switch (i) {
-	case 0: batch_bulk_kernel<N, S, 256, 4, 16><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 1: batch_bulk_kernel<N, S, 256, 2, 16><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 2: batch_bulk_kernel<N, S, 256, 4, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 3: batch_bulk_kernel<N, S, 128, 4, 32><<<grid, 128 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 4: batch_bulk_kernel<N, S, 256, 1, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 0: batch_bulk_kernel<N, S, 256, 4, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 1: batch_bulk_kernel<N, S, 256, 8, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 2: batch_bulk_kernel<N, S, 256, 4, 64><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 3: batch_bulk_kernel<N, S, 512, 2, 32><<<grid, 512 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 4: batch_bulk_kernel<N, S, 128, 8, 32><<<grid, 128 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
 	default: return cudaErrorInvalidValue;
 	}
 	return cudaGetLastError();
