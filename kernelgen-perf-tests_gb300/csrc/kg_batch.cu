@@ -509,6 +509,11 @@ __device__ __forceinline__ void bulk_copy(void* dst_smem, const void* src, unsig
 		::"r"(smem_addr(dst_smem)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
 }
 
+// The bulk kernel's dynamic shared memory (the first-tile table, then the
+// mbarriers and the rings): named at file scope so that the tile code's
+// reads are shared-memory loads with 32-bit offsets.
+extern __shared__ __align__(128) unsigned char bk_smem[];
+
 // One item (tile) of the batch as the bulk kernel walks it: NC = NT CPT
 // consecutive interior columns per step (each thread takes CPT of them, NT
 // apart); 3D: the same columns on KC planes; 2D: KC groups of NC columns.
@@ -565,9 +570,9 @@ template <class Op, class S> struct BulkChunk {
 };
 
 template <class Op, class N, class S, int NT, int CPT, int KC>
-__device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>& p, const BulkRings& rg,
-	unsigned char* sm, uint64_t* full, uint64_t* done, volatile int* abort, uint32_t& g, bool producer, int* err,
-	long long wait, bool& ok)
+__device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>& p,
+	const BulkRings& rg, unsigned char* sm, int rbase, uint64_t* full, uint64_t* done, volatile int* abort,
+	uint32_t& g, bool producer, int* err, long long wait, bool& ok)
 {
 	constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
 	constexpr Slots sl = Op::slots();
@@ -698,37 +703,38 @@ __device__ void bulk_item(const Op& op, const BatchDesc& d, int t, const Ptrs<S>
 		const long long pk = k2d ? 0 : (long long)k * it.P;
 		N o[CPT][3];
 		if (!cut) {
-			// per (input, plane): the byte offset, from the rings' base, that
-			// full index 0 of the chunk's plane would have, so that element fc
-			// lies at byte b + fc ES
-			long long b[6][5];
+			// per (input, plane): the byte offset in the dynamic shared memory
+			// of the chunk's element for full index fl (the step's first
+			// column), so that column fc lies at b + (fc - fl) ES
+			int b[6][5];
 #pragma unroll
 			for (int q = 0; q < NIN; q++) {
 				const Halo h = Op::halo(q);
-				const long long lob = fl - (h.x0 + (long long)h.y0 * it.nx);   // first needed index, plane-relative
+				const int lo_off = h.x0 + h.y0 * it.nx;
+				const long long lob = fl - lo_off;   // first needed index, plane-relative
 #pragma unroll
 				for (int m = 0; m < 5; m++) {
 					if (m >= NZ(q)) continue;
 					const int pl = k2d ? 0 : k - h.z0 + m;
 					const int phase = (int)((lob + (long long)pl * pm) & (A - 1));
 					const int slot = (k2d ? s : pl) % RZ(q);
-					b[q][m] = rg.off[q] + (long long)slot * rg.cap[q] * ES + (phase - lob) * ES;
+					b[q][m] = rbase + rg.off[q] + slot * rg.cap[q] * ES + (phase + lo_off) * ES;
 				}
 			}
+			const int nxes = it.nx * ES;
 #pragma unroll
 			for (int r = 0; r < CPT; r++) {
 				struct Acc {
-					const unsigned char* sm;
-					long long (*b)[5];
-					long long fc;
-					int nx;
+					int (*b)[5];
+					int rel;       // (fc - fl) ES
+					int nxes;
 					__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
 						return Conv<N, S>::from(raw(q, dx, dy, dz));
 					}
 					__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
-						return *reinterpret_cast<const S*>(sm + (b[q][dz + Op::halo(q).z0] + (fc + dx + dy * nx) * ES));
+						return *reinterpret_cast<const S*>(bk_smem + (b[q][dz + Op::halo(q).z0] + rel + dx * ES + dy * nxes));
 					}
-				} at{sm, b, fc[r], it.nx};
+				} at{b, (int)(fc[r] - fl) * ES, nxes};
 				op.point(at, o[r]);
 			}
 		} else {
@@ -755,8 +761,8 @@ template <class N, class S, int NT, int CPT, int KC>
 __global__ void __launch_bounds__(NT + 32, 768 / NT) batch_bulk_kernel(const BatchDesc* __restrict__ desc, int nprob, int total,
 	const long long* __restrict__ step_base, int local, BulkLayout lay, int* err, long long wait)
 {
-	extern __shared__ __align__(128) unsigned char bk_smem[];
 	int* first = reinterpret_cast<int*>(bk_smem);
+	const int rbase = tb_first_bytes(nprob);   // ring offsets count from the mbarriers
 	uint64_t* full = reinterpret_cast<uint64_t*>(bk_smem + tb_first_bytes(nprob));
 	uint64_t* done = full + kBulkNB;
 	volatile int* abort = reinterpret_cast<volatile int*>(reinterpret_cast<unsigned char*>(full) + kBulkBar - 8);
@@ -790,20 +796,20 @@ __global__ void __launch_bounds__(NT + 32, 768 / NT) batch_bulk_kernel(const Bat
 		const BulkRings& rg = lay.k[bulk_kind(d.stencil)];
 		switch (d.stencil) {
 		case KG_LAPLACIAN:
-			bulk_item<OpLaplacian<N>, N, S, NT, CPT, KC>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, d, t, p, rg, rings, full, done,
+			bulk_item<OpLaplacian<N>, N, S, NT, CPT, KC>(OpLaplacian<N>{N(d.c[0]), N(d.c[1])}, d, t, p, rg, rings, rbase, full, done,
 				abort, g, producer, err, wait, ok);
 			break;
 		case KG_DIVERGENCE:
 			bulk_item<OpDivergence<N>, N, S, NT, CPT, KC>(OpDivergence<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, t, p, rg,
-				rings, full, done, abort, g, producer, err, wait, ok);
+				rings, rbase, full, done, abort, g, producer, err, wait, ok);
 			break;
 		case KG_WAVE13PT:
 			bulk_item<OpWave13pt<N>, N, S, NT, CPT, KC>(OpWave13pt<N>{N(d.c[0]), N(d.c[1]), N(d.c[2])}, d, t, p, rg, rings,
-				full, done, abort, g, producer, err, wait, ok);
+				rbase, full, done, abort, g, producer, err, wait, ok);
 			break;
 		case KG_GAUSSBLUR:
 			bulk_item<OpGaussblur<N>, N, S, NT, CPT, KC>(OpGaussblur<N>{N(d.c[0]), N(d.c[1]), N(d.c[2]), N(d.c[3]),
-				N(d.c[4]), N(d.c[5]), N(d.c[6])}, d, t, p, rg, rings, full, done, abort, g, producer, err, wait, ok);
+				N(d.c[4]), N(d.c[5]), N(d.c[6])}, d, t, p, rg, rings, rbase, full, done, abort, g, producer, err, wait, ok);
 			break;
 		default: break;
 		}
