@@ -630,10 +630,12 @@ def run_batched(nsteps=50, reps=3, tune_cache=None):
     out["tune_s"] = round(time.perf_counter() - t0, 3)
     cfg = b32.config()
     out["tuned"] = {"config": cfg.shape, "bx": cfg.bx, "by": cfg.by, "kc": cfg.kc, "temporal": cfg.temporal,
-                    "ctas_per_sm": cfg.ctas_per_sm, "tiles": cfg.tiles, "configs_tried": cfg.nshapes,
-                    "what": "temporal == 1: tiles of bx*by threads on consecutive columns, kc planes each; "
-                            "temporal T > 1: output blocks of bx x by x kc points evaluated T steps deep in "
-                            "shared memory per launch"}
+                    "staged": cfg.staged, "ctas_per_sm": cfg.ctas_per_sm, "tiles": cfg.tiles,
+                    "configs_tried": cfg.nshapes,
+                    "what": "staged == 1: tiles of bx threads x by columns each (consecutive columns), kc planes, "
+                            "inputs staged in shared memory by bulk copies; temporal == 1 and staged == 0: tiles of "
+                            "bx*by threads on consecutive columns, kc planes each, loads through L1; temporal T > 1: "
+                            "output blocks of bx x by x kc points evaluated T steps deep in shared memory per launch"}
     restore()
     b32.set_step(0)
     b32.capture(nsteps)
