@@ -199,10 +199,17 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 }
 
 // Shared memory per CTA for the rings: L (steps of copies in flight) is the
-// largest, up to 6, whose rings fit this budget; the CTAs per SM follow from
-// what the rings then take.
+// largest, up to 6, whose rings fit the budget of the storage size; the CTAs
+// per SM follow from what the rings then take.  Measured on GB300 (Gpts/s at
+// 512x256x256 and 1024x512x512): 2-byte storage gains from more CTAs with
+// shallower rings (48 KB against 100 KB: BF16 laplacian 900 -> 985 and
+// 1236 -> 1311, gradient 400 -> 482 and 575 -> 616, the others within 1 %),
+// FP32 loses (laplacian 661 -> 546).
 #ifndef KG_TMAVEC_BUDGET
 #define KG_TMAVEC_BUDGET (100 * 1024)
+#endif
+#ifndef KG_TMAVEC_BUDGET16
+#define KG_TMAVEC_BUDGET16 (48 * 1024)
 #endif
 // Rows of points per lane (each lane evaluates PY x V points per plane):
 // measured on GB300, two rows for 2-byte storage (BF16 wave13pt 720 -> 817
@@ -213,7 +220,7 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 #endif
 template <class Op, class S, int BX, int BY> struct TmaVecDepth {
 	template <int L> static constexpr int bytes() { return TGeo<Op, S, BX, BY, L>::total(); }
-	static constexpr int kBudget = KG_TMAVEC_BUDGET;
+	static constexpr int kBudget = sizeof(S) == 2 ? KG_TMAVEC_BUDGET16 : KG_TMAVEC_BUDGET;
 	static constexpr int L = bytes<6>() <= kBudget ? 6 : bytes<5>() <= kBudget ? 5 : bytes<4>() <= kBudget ? 4
 		: bytes<3>() <= kBudget ? 3 : bytes<2>() <= kBudget ? 2 : 1;
 };
