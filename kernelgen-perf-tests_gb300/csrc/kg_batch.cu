@@ -517,34 +517,55 @@ extern __shared__ __align__(128) unsigned char bk_smem[];
 // One item (tile) of the batch as the bulk kernel walks it: NC = NT CPT
 // consecutive interior columns per step (each thread takes CPT of them, NT
 // apart); 3D: the same columns on KC planes; 2D: KC groups of NC columns.
+// The bulk path takes problems of fewer than 2^31 - 2^16 points, so every
+// index of an item (and its sums with a step's columns) is a 32-bit int.
 template <class Op> struct BulkItem {
 	static constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
-	int nx, ny, ns, dxn;
-	long long ncol, col0, P;
-	int kb, nsteps;
+	int nx, ny, ns, dxn, ncol, col0, P, kb, nsteps;
 	__device__ __forceinline__ void init(const BatchDesc& d, int t, int NC, int KC) {
 		nx = d.nx;
 		ny = d.ny;
 		ns = d.ns;
 		dxn = nx - Op::LX - Op::HX;
-		ncol = (long long)dxn * (ny - Op::LY - Op::HY);
-		P = (long long)nx * ny;
+		ncol = dxn * (ny - Op::LY - Op::HY);
+		P = nx * ny;
 		const int tcol = t % d.tiles_x, tz = t / d.tiles_x;
 		if (k2d) {
-			col0 = (long long)tcol * KC * NC;
+			col0 = tcol * KC * NC;
 			kb = 0;
-			nsteps = (int)min((long long)KC, (ncol - col0 + NC - 1) / NC);
+			nsteps = min(KC, (ncol - col0 + NC - 1) / NC);
 		} else {
-			col0 = (long long)tcol * NC;
+			col0 = tcol * NC;
 			kb = Op::LZ + tz * KC;
 			nsteps = min(KC, ns - Op::HZ - kb);
 		}
 	}
-	// full index (in its plane) of interior column col (the bulk path takes
-	// problems of fewer than 2^31 points, so 32-bit division suffices)
-	__device__ __forceinline__ long long f(long long col) const {
-		const int c = (int)col, j = c / dxn;
-		return Op::LX + (c - j * dxn) + (long long)nx * (Op::LY + j);
+	// full index (in its plane) of interior column col
+	__device__ __forceinline__ int f(int col) const {
+		const int j = col / dxn;
+		return Op::LX + (col - j * dxn) + nx * (Op::LY + j);
+	}
+};
+
+// A column of a 2D item and its full index, moved NC columns on per step
+// without a division: NC = qd dxn + rd, so a step adds rd to the column's x
+// offset and qd rows, and one more row where x passes the row's end.
+struct ColWalk {
+	int col, i, fc;   // interior column, its x offset in the row, full index
+	template <class Op> __device__ __forceinline__ void start(const BulkItem<Op>& it, int c) {
+		const int j = c / it.dxn;
+		col = c;
+		i = c - j * it.dxn;
+		fc = Op::LX + i + it.nx * (Op::LY + j);
+	}
+	__device__ __forceinline__ void step(int NC, int rd, int fq, int dxn, int wrap) {
+		col += NC;
+		i += rd;
+		fc += fq;
+		if (i >= dxn) {
+			i -= dxn;
+			fc += wrap;
+		}
 	}
 };
 
@@ -552,19 +573,18 @@ template <class Op> struct BulkItem {
 // it copies, the 16-byte phase of its first needed element, and whether the
 // array's end cut it short.
 template <class Op, class S> struct BulkChunk {
-	long long st;
-	int count, phase;
+	int st, count, phase;
 	bool cut;
-	__device__ __forceinline__ void make(int q, long long fl, long long fh, long long pbase, int nx, long long n) {
+	__device__ __forceinline__ void make(int q, int fl, int fh, int pbase, int nx, int n) {
 		constexpr int A = 16 / (int)sizeof(S);
 		const Halo h = Op::halo(q);
-		const long long lo = fl - (h.x0 + (long long)h.y0 * nx) + pbase;
-		const long long end = fh + h.x1 + (long long)h.y1 * nx + 1 + pbase;   // exclusive
-		const long long nfl = n / A * A;
-		phase = (int)(lo & (A - 1));
+		const int lo = fl - (h.x0 + h.y0 * nx) + pbase;
+		const int end = fh + h.x1 + h.y1 * nx + 1 + pbase;   // exclusive
+		const int nfl = n & ~(A - 1);
+		phase = lo & (A - 1);
 		st = lo - phase;
-		const long long e = min((end + A - 1) / A * A, nfl);
-		count = (int)max(0LL, e - st);
+		const int e = min((end + A - 1) & ~(A - 1), nfl);
+		count = max(0, e - st);
 		cut = end > nfl || count == 0;
 	}
 };
@@ -582,16 +602,23 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 	constexpr int NC = NT * CPT;
 	BulkItem<Op> it;
 	it.init(d, t, NC, KC);
-	const long long n = it.P * it.ns;
+	const int n = it.P * it.ns;
 	auto NZ = [](int q) { return k2d ? 1 : Op::halo(q).z0 + Op::halo(q).z1 + 1; };
 	auto RZ = [](int q) { return (k2d ? 1 : Op::halo(q).z0 + Op::halo(q).z1 + 1) + kBulkL; };
-	// the columns of step s: first and last full index
-	auto step_cols = [&](int s, long long& fl, long long& fh) {
-		const long long c0 = k2d ? it.col0 + (long long)s * NC : it.col0;
-		const long long c1 = min(c0 + NC, it.ncol) - 1;
-		fl = it.f(c0);
-		fh = it.f(c1);
-	};
+	// the steps' first and last columns: fixed in 3D; in 2D walked NC
+	// columns on per step (the last step's last column is the domain's)
+	const int qd = NC / it.dxn, rd = NC - qd * it.dxn;
+	const int fq = rd + qd * it.nx, wrap = it.nx - it.dxn;
+	ColWalk wl, wh;
+	int fl = 0, fh = 0, flast = 0;
+	if (k2d) {
+		wl.start(it, it.col0);
+		wh.start(it, it.col0 + NC - 1);
+		flast = it.f(it.ncol - 1);
+	} else {
+		fl = it.f(it.col0);
+		fh = it.f(min(it.col0 + NC, it.ncol) - 1);
+	}
 	if (producer) {
 		// a new item's windows may reuse any slot: wait for the previous item
 		if (g > 0 && ok) ok = mbar_wait(&done[(g - 1) % kBulkNB], ((g - 1) / kBulkNB) & 1, kTmaWaitCycles, abort);
@@ -601,8 +628,10 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 			if (s >= kBulkL + 1)
 				ok = mbar_wait(&done[(gs - kBulkL - 1) % kBulkNB], ((gs - kBulkL - 1) / kBulkNB) & 1, kTmaWaitCycles, abort);
 			if (!ok) break;
-			long long fl, fh;
-			step_cols(s, fl, fh);
+			if (k2d) {
+				fl = wl.fc;
+				fh = wh.col < it.ncol ? wh.fc : flast;
+			}
 			const int k = it.kb + s;
 			// planes of this step: the window at the first step, then the
 			// newest; the byte count first, then the copies
@@ -614,7 +643,7 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 				const int np = k2d ? 1 : (s == 0 ? NZ(q) : 1);
 				for (int m = 0; m < np; m++) {
 					BulkChunk<Op, S> ch;
-					ch.make(q, fl, fh, k2d ? 0 : (long long)(p0 + m) * it.P, it.nx, n);
+					ch.make(q, fl, fh, k2d ? 0 : (p0 + m) * it.P, it.nx, n);
 					bytes += (unsigned)ch.count * ES;
 				}
 			}
@@ -627,7 +656,7 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 				const int np = k2d ? 1 : (s == 0 ? NZ(q) : 1);
 				for (int m = 0; m < np; m++) {
 					BulkChunk<Op, S> ch;
-					ch.make(q, fl, fh, k2d ? 0 : (long long)(p0 + m) * it.P, it.nx, n);
+					ch.make(q, fl, fh, k2d ? 0 : (p0 + m) * it.P, it.nx, n);
 					const int slot = (k2d ? s : p0 + m) % RZ(q);
 					if (ch.count > 0)
 						bulk_copy(sm + rg.off[q] + slot * rg.cap[q] * ES, p.in[q] + ch.st, (unsigned)ch.count * ES,
@@ -635,6 +664,10 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 				}
 			}
 			issued = gs + 1;
+			if (k2d) {
+				wl.step(NC, rd, fq, it.dxn, wrap);
+				wh.step(NC, rd, fq, it.dxn, wrap);
+			}
 		}
 		if (!ok) {
 			// every step before the last kBulkNB issued is done; the copies of
@@ -648,29 +681,53 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 	}
 	// ---- compute warps ----
 	const int tid = threadIdx.x, lane = tid & 31;
-	// 3D: the columns, their full indices and the chunks' placement are the
-	// same on every plane of the item; whether an input's chunk reaches past
-	// the array's last whole 16 bytes is checked on the item's last window
-	long long fl = 0, fh = 0;
-	long long fc[CPT];
+	const int pm = it.P & (A - 1);
+	const int nxes = it.nx * ES;
+	// the thread's columns: 3D fixed for the item; 2D walked with the steps
+	// (a column past the domain is evaluated at the step's first column and
+	// not stored)
+	ColWalk wc[CPT];
+	int fc[CPT];
 	bool cv[CPT];
 	bool item_cut = false;
+	// per input: byte offset of the chunk of the newest plane for full index
+	// fl (all but the ring slot and the 16-byte phase), the newest plane's
+	// slot and phase, and the offsets of the NZ planes of the step
+	int qb[6], nsl[6], nph[6];
+	int b[6][5];
+#pragma unroll
+	for (int q = 0; q < NIN; q++) {
+		const Halo h = Op::halo(q);
+		qb[q] = rbase + rg.off[q] + (h.x0 + h.y0 * it.nx) * ES;
+	}
 	if (!k2d) {
-		step_cols(0, fl, fh);
 #pragma unroll
 		for (int r = 0; r < CPT; r++) {
-			const long long col = it.col0 + tid + r * NT;
+			const int col = it.col0 + tid + r * NT;
 			cv[r] = col < it.ncol;
 			fc[r] = it.f(cv[r] ? col : it.col0);
 		}
 #pragma unroll
 		for (int q = 0; q < NIN; q++) {
+			const Halo h = Op::halo(q);
 			BulkChunk<Op, S> ch;
-			ch.make(q, fl, fh, (long long)(it.kb + it.nsteps - 1 + Op::halo(q).z1) * it.P, it.nx, n);
+			ch.make(q, fl, fh, (it.kb + it.nsteps - 1 + h.z1) * it.P, it.nx, n);
 			item_cut = item_cut || ch.cut;
+			// the planes of step 0: kb - z0 .. kb + z1
+			const int lob = fl - (h.x0 + h.y0 * it.nx);
+#pragma unroll
+			for (int m = 0; m < 5; m++) {
+				if (m >= NZ(q)) continue;
+				const int pl = it.kb - h.z0 + m;
+				nph[q] = (lob + pl * pm) & (A - 1);
+				nsl[q] = pl % RZ(q);
+				b[q][m] = qb[q] + (nsl[q] * rg.cap[q] + nph[q]) * ES;
+			}
 		}
+	} else {
+#pragma unroll
+		for (int r = 0; r < CPT; r++) wc[r].start(it, it.col0 + tid + r * NT);
 	}
-	const int pm = (int)(it.P & (A - 1));
 	for (int s = 0; s < it.nsteps; s++) {
 		const uint32_t gs = g + s;
 		const bool got = __all_sync(0xffffffffu, mbar_wait(&full[gs % kBulkNB], (gs / kBulkNB) & 1, wait, abort));
@@ -682,50 +739,35 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 			ok = false;
 			return;
 		}
-		const int k = it.kb + s;
 		bool cut = item_cut;
 		if (k2d) {
-			step_cols(s, fl, fh);
-			const long long c0 = it.col0 + (long long)s * NC;
+			fl = wl.fc;
+			fh = wh.col < it.ncol ? wh.fc : flast;
 #pragma unroll
 			for (int r = 0; r < CPT; r++) {
-				const long long col = c0 + tid + r * NT;
-				cv[r] = col < it.ncol;
-				fc[r] = it.f(cv[r] ? col : c0);
+				cv[r] = wc[r].col < it.ncol;
+				fc[r] = cv[r] ? wc[r].fc : fl;
 			}
-#pragma unroll
-			for (int q = 0; q < NIN; q++) {
-				BulkChunk<Op, S> ch;
-				ch.make(q, fl, fh, 0, it.nx, n);
-				cut = cut || ch.cut;
-			}
-		}
-		const long long pk = k2d ? 0 : (long long)k * it.P;
-		N o[CPT][3];
-		if (!cut) {
-			// per (input, plane): the byte offset in the dynamic shared memory
-			// of the chunk's element for full index fl (the step's first
-			// column), so that column fc lies at b + (fc - fl) ES
-			int b[6][5];
+			const int slot = s % RZ(0);
 #pragma unroll
 			for (int q = 0; q < NIN; q++) {
 				const Halo h = Op::halo(q);
-				const int lo_off = h.x0 + h.y0 * it.nx;
-				const long long lob = fl - lo_off;   // first needed index, plane-relative
-#pragma unroll
-				for (int m = 0; m < 5; m++) {
-					if (m >= NZ(q)) continue;
-					const int pl = k2d ? 0 : k - h.z0 + m;
-					const int phase = (int)((lob + (long long)pl * pm) & (A - 1));
-					const int slot = (k2d ? s : pl) % RZ(q);
-					b[q][m] = rbase + rg.off[q] + slot * rg.cap[q] * ES + (phase + lo_off) * ES;
-				}
+				BulkChunk<Op, S> ch;
+				ch.make(q, fl, fh, 0, it.nx, n);
+				cut = cut || ch.cut;
+				b[q][0] = qb[q] + (slot * rg.cap[q] + ch.phase) * ES;
 			}
-			const int nxes = it.nx * ES;
+		}
+		const long long pk = k2d ? 0 : (long long)(it.kb + s) * it.P;
+		N o[CPT][3];
+		if (!cut) {
+			// input q's value at column fc, offset (dx, dy, dz), lies at byte
+			// b[q][dz + z0] + (fc - fl) ES + dx ES + dy nx ES of the dynamic
+			// shared memory
 #pragma unroll
 			for (int r = 0; r < CPT; r++) {
 				struct Acc {
-					int (*b)[5];
+					const int (*b)[5];
 					int rel;       // (fc - fl) ES
 					int nxes;
 					__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
@@ -734,7 +776,7 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 					__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
 						return *reinterpret_cast<const S*>(bk_smem + (b[q][dz + Op::halo(q).z0] + rel + dx * ES + dy * nxes));
 					}
-				} at{b, (int)(fc[r] - fl) * ES, nxes};
+				} at{b, (fc[r] - fl) * ES, nxes};
 				op.point(at, o[r]);
 			}
 		} else {
@@ -748,17 +790,39 @@ __device__ __forceinline__ void bulk_item(const Op& op, const BatchDesc& d, int 
 		__syncwarp();
 		if (lane == 0) mbar_arrive(&done[gs % kBulkNB]);
 #pragma unroll
-		for (int r = 0; r < CPT; r++)
-			if (cv[r])
+		for (int q = 0; q < sl.nout; q++) {
+			S* out = p.out[q] + pk;
 #pragma unroll
-				for (int q = 0; q < sl.nout; q++) p.out[q][fc[r] + pk] = Conv<N, S>::to(o[r][q]);
+			for (int r = 0; r < CPT; r++)
+				if (cv[r]) out[fc[r]] = Conv<N, S>::to(o[r][q]);
+		}
+		// the next step's planes: the window moves one plane on
+		if (k2d) {
+			wl.step(NC, rd, fq, it.dxn, wrap);
+			wh.step(NC, rd, fq, it.dxn, wrap);
+#pragma unroll
+			for (int r = 0; r < CPT; r++) wc[r].step(NC, rd, fq, it.dxn, wrap);
+		} else {
+#pragma unroll
+			for (int q = 0; q < NIN; q++) {
+#pragma unroll
+				for (int m = 0; m + 1 < 5; m++)
+					if (m + 1 < NZ(q)) b[q][m] = b[q][m + 1];
+				nsl[q] = nsl[q] + 1 == RZ(q) ? 0 : nsl[q] + 1;
+				nph[q] = (nph[q] + pm) & (A - 1);
+				b[q][NZ(q) - 1] = qb[q] + (nsl[q] * rg.cap[q] + nph[q]) * ES;
+			}
+		}
 	}
 	g += it.nsteps;
 }
 
-// Registers bounded for three CTAs of 256 compute threads per SM.
+// Registers bounded for the CTAs per SM the rings leave room for: two of
+// 512 compute threads, four of 256 with two columns each, three of 256 with
+// four.
+constexpr int bulk_min_blocks(int nt, int cpt) { return nt >= 512 ? 2 : cpt <= 2 ? 4 : 3; }
 template <class N, class S, int NT, int CPT, int KC>
-__global__ void __launch_bounds__(NT + 32, 768 / NT) batch_bulk_kernel(const BatchDesc* __restrict__ desc, int nprob, int total,
+__global__ void __launch_bounds__(NT + 32, bulk_min_blocks(NT, CPT)) batch_bulk_kernel(const BatchDesc* __restrict__ desc, int nprob, int total,
 	const long long* __restrict__ step_base, int local, BulkLayout lay, int* err, long long wait)
 {
 	int* first = reinterpret_cast<int*>(bk_smem);
@@ -843,7 +907,7 @@ static const int k_ntb = sizeof(k_tb_shapes) / sizeof(k_tb_shapes[0]);
 // Bulk-staged one-step tiles (NT consecutive columns, KC planes); configuration
 // index k_nshapes + k_ntb + i.
 struct BulkShape { int nt, cpt, kc; };
-static const BulkShape k_bulk_shapes[] = {{256, 4, 32}, {256, 8, 32}, {256, 4, 64}, {512, 2, 32}, {128, 8, 32}};
+static const BulkShape k_bulk_shapes[] = {{256, 4, 32}, {512, 2, 64}, {256, 4, 64}, {512, 2, 32}, {256, 2, 64}, {256, 2, 32}};
 static const int k_nbulk = sizeof(k_bulk_shapes) / sizeof(k_bulk_shapes[0]);
 static const int k_bulk0 = k_nshapes + k_ntb;
 static const int k_nconfigs = k_nshapes + k_ntb + k_nbulk;
@@ -973,7 +1037,7 @@ static int tb_occupancy(size_t smem)
 // (the NT columns' span, grown by the input's reach, plus 16-byte rounding at
 // both ends); NZ + kBulkL slots per input.  Returns the dynamic shared memory
 // (first-tile table, mbarriers, rings), 0 if an array is not 16-byte aligned
-// or a problem has 2^31 points or more.
+// or a problem has 2^31 - 2^16 points or more.
 template <class Op> static void bulk_rings_of(const kg_problem& p, int nt, int es, BulkRings& r, int& bytes)
 {
 	constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
@@ -1002,7 +1066,7 @@ static size_t bulk_layout(const std::vector<kg_problem>& probs, int es, int nt, 
 	int bytes[4] = {kBulkBar, kBulkBar, kBulkBar, kBulkBar};
 	for (const kg_problem& p : probs) {
 		const long long n = (long long)p.nx * p.ny * p.ns;
-		if (n >= (1LL << 31)) return 0;
+		if (n >= (1LL << 31) - (1LL << 16)) return 0;
 		for (int k = 0; k < kg_stencil_narrays(p.stencil); k++)
 			if ((uintptr_t)p.arr[k] % 16) return 0;
 	}
@@ -1044,10 +1108,11 @@ static int bulk_occupancy(int i, size_t smem)
 {
 	switch (i) {
 	case 0: return bulk_occ<N, S, 256, 4, 32>(smem);
-	case 1: return bulk_occ<N, S, 256, 8, 32>(smem);
+	case 1: return bulk_occ<N, S, 512, 2, 64>(smem);
 	case 2: return bulk_occ<N, S, 256, 4, 64>(smem);
 	case 3: return bulk_occ<N, S, 512, 2, 32>(smem);
-	case 4: return bulk_occ<N, S, 128, 8, 32>(smem);
+	case 4: return bulk_occ<N, S, 256, 2, 64>(smem);
+	case 5: return bulk_occ<N, S, 256, 2, 32>(smem);
 	default: return 0;
 	}
 }
@@ -1058,10 +1123,11 @@ static cudaError_t bulk_launch(int i, dim3 grid, size_t smem, const BatchDesc* d
 {
 	switch (i) {
 	case 0: batch_bulk_kernel<N, S, 256, 4, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 1: batch_bulk_kernel<N, S, 256, 8, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 1: batch_bulk_kernel<N, S, 512, 2, 64><<<grid, 512 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
 	case 2: batch_bulk_kernel<N, S, 256, 4, 64><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
 	case 3: batch_bulk_kernel<N, S, 512, 2, 32><<<grid, 512 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
-	case 4: batch_bulk_kernel<N, S, 128, 8, 32><<<grid, 128 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 4: batch_bulk_kernel<N, S, 256, 2, 64><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
+	case 5: batch_bulk_kernel<N, S, 256, 2, 32><<<grid, 256 + 32, smem, st>>>(desc, nprob, total, base, local, lay, err, wait); break;
 	default: return cudaErrorInvalidValue;
 	}
 	return cudaGetLastError();
@@ -1261,6 +1327,10 @@ static std::string batch_signature(const kg_batch_s* b)
 	auto mix = [&](long long v) { h ^= (unsigned long long)v; h *= 1099511628211ULL; };
 	mix(b->dtype);
 	for (const kg_problem& p : b->probs) { mix(p.stencil); mix(p.nx); mix(p.ny); mix(p.ns); }
+	// the configuration table: a cached index means nothing for another table
+	for (const Shape& c : k_shapes) { mix(c.bx); mix(c.by); mix(c.kc); }
+	for (const TBShape& c : k_tb_shapes) { mix(c.bx); mix(c.by); mix(c.bz); mix(c.t); }
+	for (const BulkShape& c : k_bulk_shapes) { mix(c.nt); mix(c.cpt); mix(c.kc); mix(bulk_min_blocks(c.nt, c.cpt)); }
 	cudaDeviceProp prop;
 	int dev = 0;
 	cudaGetDevice(&dev);
