@@ -344,11 +344,12 @@ kg_status kg_batch_step(kg_batch b, int nsteps, kg_stream_t stream);
  * kg_batch_launch replays it and continues from the current step. */
 kg_status kg_batch_capture(kg_batch b, int nsteps);
 kg_status kg_batch_launch(kg_batch b, kg_stream_t stream);
-/* Times every configuration -- the one-step tile shapes and the temporal
- * blocks with their factors T = 2, 3, 4 -- with as many CTAs per SM as stay
- * resident, one fewer and half as many, on this batch (advancing it), and
- * keeps the fastest; cache_path (may be NULL) stores and reuses the choice
- * per device and problem list. */
+/* Times every configuration -- the one-step tile shapes, the temporal
+ * blocks with their factors T = 2, 3, 4 and the bulk-staged tiles -- with as
+ * many CTAs per SM as stay resident, one fewer, half as many, twice and four
+ * times as many (up to 32), on this batch (advancing it), and keeps the
+ * fastest; cache_path (may be NULL) stores and reuses the choice per device,
+ * problem list and configuration table. */
 kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream);
 kg_status kg_batch_set_config(kg_batch b, int shape, int ctas_per_sm);
 kg_status kg_batch_get_config(kg_batch b, kg_batch_config* cfg);

@@ -1502,7 +1502,7 @@ kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream)
 	// Each trial advances the batch; the roles stay consistent because the
 	// device step counter advances with them.
 	for (int sh = 0; sh < k_nconfigs && s == KG_OK; sh++) {
-		// one wave of resident CTAs, one fewer per SM, half as many
+		// one wave of resident CTAs, one fewer per SM, half as many,
 		int occ;
 		if (sh < k_nshapes) {
 			occ = b->dtype == KG_F32 ? shape_occupancy<FF, float>(sh) : shape_occupancy<SD, double>(sh);
@@ -1520,9 +1520,18 @@ kg_status kg_batch_tune(kg_batch b, const char* cache_path, kg_stream_t stream)
 			occ = b->dtype == KG_F32 ? tb_occupancy<FF, float>(smem) : tb_occupancy<SD, double>(smem);
 			if (occ < 1) continue;
 		}
-		int cand[3] = {occ, occ > 1 ? occ - 1 : 1, occ > 1 ? occ / 2 : 1};
-		for (int c = 0; c < 3 && s == KG_OK; c++) {
-			if (c > 0 && (cand[c] == cand[c - 1] || (c == 2 && cand[2] == cand[0]))) continue;
+		// and 2x and 4x a wave: CTAs beyond the resident ones start as others
+		// finish, so the hardware hands out the last items to whichever SM is
+		// free (a persistent wave keeps its static share of uneven items)
+		const int want[5] = {occ, occ - 1, occ / 2, 2 * occ, 4 * occ};
+		int cand[5], nc = 0;
+		for (int w : want) {
+			const int c = std::min(std::max(w, 1), 32);
+			bool seen = false;
+			for (int q = 0; q < nc; q++) seen = seen || cand[q] == c;
+			if (!seen) cand[nc++] = c;
+		}
+		for (int c = 0; c < nc && s == KG_OK; c++) {
 			if ((s = kg_batch_set_config(b, sh, cand[c])) != KG_OK) break;
 			if ((s = kg_batch_step(b, 1, stream)) != KG_OK) break;  // warm-up
 			cudaEventRecord(e0, st);

@@ -61,6 +61,45 @@ def test_solve_to_tolerance(kind):
     assert not g[0].any() and not g[-1].any() and not g[:, 0].any() and not g[:, :, -1].any()
 
 
+def fp32_rbsor(e, r, shape, omega, sweeps):
+    """FP32 red-black SOR on A e = r in place (numpy float32, one rounding per
+    operation, the GPU sweep's operand order): colour 0 then colour 1, each
+    colour's points read only the other colour."""
+    nx, ny, ns = shape
+    g = e.reshape(ns, ny, nx)
+    rr = r.reshape(ns, ny, nx)
+    k, j, i = np.meshgrid(np.arange(ns), np.arange(ny), np.arange(nx), indexing="ij")
+    inner = (i > 0) & (i < nx - 1) & (j > 0) & (j < ny - 1) & (k > 0) & (k < ns - 1)
+    w, sixth = np.float32(omega), np.float32(1.0 / 6.0)
+    for _ in range(sweeps):
+        for color in (0, 1):
+            mask = inner & (((i + j + k) & 1) == color)
+            s = np.zeros_like(g)
+            s[1:-1, 1:-1, 1:-1] = (((((g[1:-1, 1:-1, :-2] + g[1:-1, 1:-1, 2:]) + g[1:-1, :-2, 1:-1]) +
+                                     g[1:-1, 2:, 1:-1]) + g[:-2, 1:-1, 1:-1]) + g[2:, 1:-1, 1:-1])
+            new = g + w * ((s + rr) * sixth - g)
+            g[mask] = new[mask]
+
+
+@pytest.mark.parametrize("shape", [(21, 18, 16), (20, 17, 15), (5, 4, 3)])
+def test_refinement_sweeps_match_fp32_restatement(shape):
+    """One outer step of refinement from u = 0: e relaxed by FP32 red-black SOR
+    on the colour-split layout, then u = e.  Equal to the FP32 restatement up
+    to FMA contraction (a wrong neighbour or colour would be O(1) off); odd and
+    even nx (the split rows' padding)."""
+    m = 6
+    f = poisson_rhs(shape)
+    fd = torch.from_numpy(f).cuda()
+    ud = torch.zeros_like(fd)
+    st, rep = kgb200.poisson_solve(shape, fd.data_ptr(), ud.data_ptr(), kgb200.KG_SOLVE_IR_SOR_F32, omega=1.8,
+                                   rtol=1e-30, sweeps_per_check=m, max_sweeps=m, raise_on_timeout=False)
+    assert st == 4 and rep.sweeps == m and rep.outer == 1
+    e = np.zeros(f.size, np.float32)
+    fp32_rbsor(e, f.astype(np.float32), shape, 1.8, m)
+    u = ud.cpu().numpy()
+    assert np.max(np.abs(u - e.astype(np.float64))) <= 1e-5 * max(np.max(np.abs(e)), 1e-30)
+
+
 def test_refinement_keeps_the_sor_rate():
     """Refinement with FP32 inner SOR needs about as many sweeps as FP64 SOR."""
     shape = (48, 40, 32)
