@@ -17,6 +17,7 @@
 #pragma once
 
 #include <algorithm>
+#include <type_traits>
 
 #include "kg_tma.cuh"
 
@@ -36,33 +37,69 @@ __device__ __forceinline__ S vrow_load(const unsigned char* b, int row_elems, in
 	return pk.v[x % V];
 }
 
+// The same value as FP32 arithmetic reads it.  BF16 is the upper half of
+// an FP32 pattern: the element is taken from the 16-byte vector's 32-bit
+// word by one shift or mask (the conversion, exactly), no 16-bit extract.
+template <class N, class S, int V>
+__device__ __forceinline__ N vrow_value(const unsigned char* b, int row_elems, int x)
+{
+	if constexpr (std::is_same<S, __nv_bfloat16>::value) {
+		const int chunk = x / V - 1;
+		const uint4 q = *reinterpret_cast<const uint4*>(b + (row_elems + chunk * V) * (int)sizeof(S));
+		const int e = x % V;
+		const uint32_t w = e / 2 == 0 ? q.x : e / 2 == 1 ? q.y : e / 2 == 2 ? q.z : q.w;
+		return mkf(__uint_as_float(e % 2 ? (w & 0xffff0000u) : (w << 16)));
+	} else {
+		return Conv<N, S>::from(vrow_load<S, V>(b, row_elems, x));
+	}
+}
+
 template <class Op, class N, class S, class G, int V, int VI, int RY = 0> struct VAcc {
 	static constexpr int ZS = 5;
 	const unsigned char* (*base)[ZS];   // per input and dz + z0: the lane's first column in the point's row
 	const S* const* in;
 	long long c, sy, sz;                      // c: the lane's first point
 	__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
-		return Conv<N, S>::from(vrow_load<S, V>(base[q][dz + Op::halo(q).z0], (dy + RY) * G::W(q), VI + dx + V));
+		return vrow_value<N, S, V>(base[q][dz + Op::halo(q).z0], (dy + RY) * G::W(q), VI + dx + V);
 	}
 	__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
 		return __ldg(in[q] + c + VI + dx + (dy + RY) * sy + dz * sz);
 	}
 };
 
-// V outputs of one lane to global memory: one vector store where all V
-// points are in the domain, else one store per point that is.
-template <class S, int V>
-__device__ __forceinline__ void vstore(S* dst, const S (&o)[V], unsigned valid_mask)
+// Two FP32 results rounded to the storage type as one packed pair (one
+// conversion instruction for both; each rounded to nearest as alone).
+template <class S> struct PairConv;
+template <> struct PairConv<__nv_bfloat16> {
+	static __device__ __forceinline__ __nv_bfloat162 to(float a, float b) { return __floats2bfloat162_rn(a, b); }
+};
+template <> struct PairConv<__half> {
+	static __device__ __forceinline__ __half2 to(float a, float b) { return __floats2half2_rn(a, b); }
+};
+
+// V outputs of one lane (FP32 arithmetic) to global memory: one vector store
+// where all V points are in the domain, else one store per point that is.
+template <class N, class S, int V>
+__device__ __forceinline__ void vstore(S* dst, const N (&o)[V], unsigned valid_mask)
 {
 	if (valid_mask == (1u << V) - 1) {
 		VPack<S, V> pk;
+		if constexpr (sizeof(S) == 2) {
+			static_assert(V % 2 == 0, "pairs");
 #pragma unroll
-		for (int v = 0; v < V; v++) pk.v[v] = o[v];
+			for (int v = 0; v < V; v += 2) {
+				const auto two = PairConv<S>::to(o[v].v, o[v + 1].v);
+				memcpy(&pk.v[v], &two, 2 * sizeof(S));
+			}
+		} else {
+#pragma unroll
+			for (int v = 0; v < V; v++) pk.v[v] = Conv<N, S>::to(o[v]);
+		}
 		*reinterpret_cast<VPack<S, V>*>(dst) = pk;
 	} else {
 #pragma unroll
 		for (int v = 0; v < V; v++)
-			if ((valid_mask >> v) & 1u) dst[v] = o[v];
+			if ((valid_mask >> v) & 1u) dst[v] = Conv<N, S>::to(o[v]);
 	}
 }
 
@@ -167,7 +204,7 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 						base[q][d] = sm + G::offset(q) + G::step_slot(q, s0[q], d - h.z0) * G::PS(q) + toff[q];
 			}
 			const long long c = c0 + sz * s;
-			S o[PY][3][V];
+			N o[PY][3][V];
 			for_v<0, PY>([&](auto ri) {
 				constexpr int R = decltype(ri)::value;
 				for_v<0, V>([&](auto vi) {
@@ -176,7 +213,7 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 					N r[3];
 					op.point(at, r);
 #pragma unroll
-					for (int q = 0; q < sl.nout; q++) o[R][q][VI] = Conv<N, S>::to(r[q]);
+					for (int q = 0; q < sl.nout; q++) o[R][q][VI] = r[q];
 				});
 			});
 			// this warp is done with the step's planes
@@ -186,7 +223,7 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 			for (int r = 0; r < PY; r++)
 				if (valid[r]) {
 #pragma unroll
-					for (int q = 0; q < sl.nout; q++) vstore<S, V>(p.out[q] + c + r * RB * sy, o[r][q], valid[r]);
+					for (int q = 0; q < sl.nout; q++) vstore<N, S, V>(p.out[q] + c + r * RB * sy, o[r][q], valid[r]);
 				}
 			if (++bi == NB) {
 				bi = 0;
@@ -217,6 +254,10 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 // 242 with two; the others within 2 %).
 #ifndef KG_TMAVEC_PY
 #define KG_TMAVEC_PY 0
+#endif
+// Runs along z per tile column (0: the TMA engine's wave-count model).
+#ifndef KG_TMAVEC_ZRUNS
+#define KG_TMAVEC_ZRUNS 0
 #endif
 template <class Op, class S, int BX, int BY> struct TmaVecDepth {
 	template <int L> static constexpr int bytes() { return TGeo<Op, S, BX, BY, L>::total(); }
@@ -303,7 +344,9 @@ struct TmaVecLaunch {
 			// z split into runs so that the CTAs fill whole waves (all tiles
 			// then walk the same planes at about the same time, and the halo
 			// rows of neighbouring tiles are served from L2)
-			const int kc = tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX());
+			constexpr int zruns = KG_TMAVEC_ZRUNS > 0 ? KG_TMAVEC_ZRUNS : 1;
+			const int kc = KG_TMAVEC_ZRUNS > 0 ? (dz + zruns - 1) / zruns
+				: tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX());
 			const int nz = (dz + kc - 1) / kc;
 			for (int y0 = 0; y0 < gy; y0 += 65535) {
 				dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
