@@ -52,6 +52,77 @@ __global__ void __launch_bounds__(kSX * kSY) rb_sor_kernel(T* __restrict__ u, co
 	}
 }
 
+// The FP32 correction of refinement is stored split by colour: point
+// (i, j, k) of colour c = (i + j + k) & 1 lives in array c, row (j, k),
+// position i >> 1 (rows of nh >= (nx + 1) / 2 elements, a multiple of 4).  In row (j, k) the
+// points of colour c are i = p + 2m, p = (c + j + k) & 1; their six
+// neighbours all have the other colour: (i - 1, j, k) and (i + 1, j, k) at
+// positions m - 1 + p and m + p of the other array's same row, the four
+// others at position m of its neighbouring rows.  A colour's sweep then
+// reads the other colour's array, its own and its right-hand side with
+// unit stride and writes only its own: 16 bytes a point per red-black sweep,
+// where the interleaved layout moves 24 (the stride-2 writes and
+// right-hand-side reads of each colour touch every sector of the array).
+// Same operands, order and expression as rb_sor_kernel.
+// A lane takes kSV consecutive positions of a row as one 16-byte vector of
+// each array (rows of nh elements, nh a multiple of kSV, so every vector is
+// aligned); the one x neighbour outside its vector is the last value of the
+// previous lane's (p = 0) or the first of the next lane's (p = 1) other-colour
+// vector, exchanged by a warp shuffle; the first and last lane of the warp
+// load theirs.  The warp's lanes share j and k, so p, the shuffles and the
+// loop trip counts are uniform across the warp.  Positions outside the
+// interior keep their values (the lane writes its whole vector: no other
+// thread writes that colour's positions in this pass).
+constexpr int kSV = 4;
+__global__ void __launch_bounds__(kSX * kSY) rb_sor_split_kernel(float* __restrict__ own,
+	const float* __restrict__ oth, const float* __restrict__ rhs, int nx, int ny, int ns, int nh, float omega,
+	int color)
+{
+	const long long rz = (long long)ny * nh;
+	const float sixth = 1.0f / 6.0f;
+	const int lane = threadIdx.x;
+	const int m0 = (blockIdx.x * kSX + lane) * kSV;
+	const bool inrow = m0 < nh;
+	auto ld = [](const float* q) { return *reinterpret_cast<const float4*>(q); };
+	for (int k = 1 + blockIdx.z; k < ns - 1; k += gridDim.z) {
+		for (int j = 1 + blockIdx.y * kSY + threadIdx.y; j < ny - 1; j += gridDim.y * kSY) {
+			const int p = (color + j + k) & 1;
+			const int mlo = 1 - p, mhi = (nx - 2 - p) >> 1;   // interior positions: i = p + 2m in [1, nx-2]
+			const long long rb = (long long)k * rz + (long long)j * nh;
+			float4 c = make_float4(0.f, 0.f, 0.f, 0.f), jm = c, jp = c, km = c, kp = c, o = c, r = c;
+			if (inrow) {
+				c = ld(oth + rb + m0);
+				jm = ld(oth + rb - nh + m0);
+				jp = ld(oth + rb + nh + m0);
+				km = ld(oth + rb - rz + m0);
+				kp = ld(oth + rb + rz + m0);
+				o = ld(own + rb + m0);
+				r = ld(rhs + rb + m0);
+			}
+			float left = __shfl_up_sync(0xffffffffu, c.w, 1), right = __shfl_down_sync(0xffffffffu, c.x, 1);
+			if (lane == 0 && p == 0 && m0 > 0 && inrow) left = oth[rb + m0 - 1];
+			if (lane == kSX - 1 && p == 1 && m0 + kSV < nh) right = oth[rb + m0 + kSV];
+			if (!inrow || m0 > mhi || m0 + kSV - 1 < mlo) continue;
+			// x neighbours (i - 1, i + 1) of position m0 + v: other-colour
+			// positions m0 + v - 1 + p and m0 + v + p
+			const float xl[kSV] = {p ? c.x : left, p ? c.y : c.x, p ? c.z : c.y, p ? c.w : c.z};
+			const float xr[kSV] = {p ? c.y : c.x, p ? c.z : c.y, p ? c.w : c.z, p ? right : c.w};
+			const float cj0[kSV] = {jm.x, jm.y, jm.z, jm.w}, cj1[kSV] = {jp.x, jp.y, jp.z, jp.w};
+			const float ck0[kSV] = {km.x, km.y, km.z, km.w}, ck1[kSV] = {kp.x, kp.y, kp.z, kp.w};
+			const float rr[kSV] = {r.x, r.y, r.z, r.w};
+			float ov[kSV] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+			for (int v = 0; v < kSV; v++) {
+				const int m = m0 + v;
+				if (m < mlo || m > mhi) continue;
+				const float s = xl[v] + xr[v] + cj0[v] + cj1[v] + ck0[v] + ck1[v];
+				ov[v] = ov[v] + omega * ((s + rr[v]) * sixth - ov[v]);
+			}
+			*reinterpret_cast<float4*>(own + rb + m0) = make_float4(ov[0], ov[1], ov[2], ov[3]);
+		}
+	}
+}
+
 // e1 = (sum of e0's face neighbours + rhs) / 6 on the interior.
 __global__ void __launch_bounds__(kSX * kSY) jacobi_kernel(const float* __restrict__ e0, float* __restrict__ e1,
 	const float* __restrict__ rhs, int nx, int ny, int ns)
@@ -70,10 +141,12 @@ __global__ void __launch_bounds__(kSX * kSY) jacobi_kernel(const float* __restri
 }
 
 // r = f - A u on the interior (FP64); r32 = (float) r (0 on the outer
-// planes); partial[b] = this block's sum of r^2.
+// planes), interleaved (nh = 0) or split by colour (rows of nh elements);
+// partial[b] = this block's sum of r^2.
 __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict__ u, const double* __restrict__ f,
-	float* __restrict__ r32, double* __restrict__ partial, int nx, int ny, int ns)
+	float* __restrict__ r32, double* __restrict__ partial, int nx, int ny, int ns, int nh)
 {
+	const long long half = (long long)nh * ny * ns;
 	__shared__ double sh[256];
 	const long long sy = nx, sz = (long long)nx * ny;
 	const long long n = sz * ns;
@@ -87,7 +160,10 @@ __global__ void __launch_bounds__(256) residual_kernel(const double* __restrict_
 			const double au = 6.0 * u[c] - (u[c - 1] + u[c + 1] + u[c - sy] + u[c + sy] + u[c - sz] + u[c + sz]);
 			r = f[c] - au;
 		}
-		if (r32) r32[c] = (float)r;
+		if (r32) {
+			if (nh) r32[((i + j + k) & 1) * half + jk * nh + (i >> 1)] = (float)r;
+			else r32[c] = (float)r;
+		}
 		acc += r * r;
 	}
 	sh[threadIdx.x] = acc;
@@ -135,22 +211,32 @@ __global__ void __launch_bounds__(256) sum_partials(const double* __restrict__ p
 	if (threadIdx.x == 0) *out = sh[0];
 }
 
-// u += e on every point (e is 0 on the outer planes).
-__global__ void axpy_kernel(double* __restrict__ u, const float* __restrict__ e, long long n)
+// u += e on every point (e is 0 on the outer planes), e interleaved
+// (nh = 0) or split by colour (rows of nh elements).
+__global__ void axpy_kernel(double* __restrict__ u, const float* __restrict__ e, int nx, int ny, int ns, int nh)
 {
-	for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
-		u[c] += (double)e[c];
+	const long long n = (long long)nx * ny * ns, half = (long long)nh * ny * ns;
+	for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+		if (nh) {
+			const int i = (int)(c % nx);
+			const long long jk = c / nx;
+			const int j = (int)(jk % ny), k = (int)(jk / ny);
+			u[c] += (double)e[((i + j + k) & 1) * half + jk * nh + (i >> 1)];
+		} else {
+			u[c] += (double)e[c];
+		}
+	}
 }
 
 struct Grid3 { dim3 grid, block; };
 
-static Grid3 sweep_grid(int nx, int ny, int ns, bool pairs)
+static Grid3 sweep_grid(int nx, int ny, int ns, bool pairs, int kz = 1)
 {
 	const int wx = pairs ? (nx - 2 + 1) / 2 : nx - 2;
 	Grid3 g;
 	g.block = dim3(kSX, kSY, 1);
 	g.grid = dim3((unsigned)std::max(1, (wx + kSX - 1) / kSX), (unsigned)std::min(std::max(1, (ny - 2 + kSY - 1) / kSY), 65535),
-		(unsigned)std::min(std::max(1, ns - 2), 65535));
+		(unsigned)std::min(std::max(1, (ns - 2 + kz - 1) / kz), 65535));
 	return g;
 }
 
@@ -173,6 +259,10 @@ extern "C" kg_status kg_poisson_solve(int nx, int ny, int ns, const double* f, d
 	cudaStream_t st = (cudaStream_t)stream;
 	const bool ir = opts->kind != KG_SOLVE_SOR_F64;
 	const bool jac = opts->kind == KG_SOLVE_IR_JACOBI_F32;
+	// refinement around SOR keeps e and its right-hand side split by colour
+	const int nh = ir && !jac ? ((nx + 1) / 2 + kSV - 1) / kSV * kSV : 0;
+	const long long half = (long long)nh * ny * ns;
+	const long long ne = nh ? 2 * half : n;
 
 	float *e = nullptr, *e2 = nullptr, *r32 = nullptr;
 	double *partial = nullptr, *norm = nullptr;
@@ -180,8 +270,8 @@ extern "C" kg_status kg_poisson_solve(int nx, int ny, int ns, const double* f, d
 	memset(&R, 0, sizeof(R));
 	kg_status s = KG_OK;
 	cudaError_t err = cudaMallocAsync((void**)&partial, sizeof(double) * (kNormBlocks + 2), st);
-	if (err == cudaSuccess && ir) err = cudaMallocAsync((void**)&e, sizeof(float) * n, st);
-	if (err == cudaSuccess && ir) err = cudaMallocAsync((void**)&r32, sizeof(float) * n, st);
+	if (err == cudaSuccess && ir) err = cudaMallocAsync((void**)&e, sizeof(float) * ne, st);
+	if (err == cudaSuccess && ir) err = cudaMallocAsync((void**)&r32, sizeof(float) * ne, st);
 	if (err == cudaSuccess && jac) err = cudaMallocAsync((void**)&e2, sizeof(float) * n, st);
 	if (err != cudaSuccess) {
 		s = fail_cuda(err, "kg_poisson_solve: work arrays");
@@ -199,10 +289,12 @@ extern "C" kg_status kg_poisson_solve(int nx, int ny, int ns, const double* f, d
 		const double fnorm = std::sqrt(host[0]);
 		R.fnorm = fnorm;
 		const Grid3 gp = sweep_grid(nx, ny, ns, true), gj = sweep_grid(nx, ny, ns, false);
+		Grid3 gs = sweep_grid(nx, ny, ns, true);
+		gs.grid.x = (unsigned)std::max(1, (nh + kSX * kSV - 1) / (kSX * kSV));
 		long long sweeps = 0;
 		for (;;) {
 			// FP64 residual (and, for refinement, its FP32 copy as the right-hand side)
-			residual_kernel<<<kNormBlocks, 256, 0, st>>>(u, f, ir ? r32 : nullptr, partial, nx, ny, ns);
+			residual_kernel<<<kNormBlocks, 256, 0, st>>>(u, f, ir ? r32 : nullptr, partial, nx, ny, ns, nh);
 			sum_partials<<<1, 256, 0, st>>>(partial, kNormBlocks, norm);
 			err = cudaMemcpyAsync(host, norm, sizeof(double), cudaMemcpyDeviceToHost, st);
 			if (err == cudaSuccess) err = cudaStreamSynchronize(st);
@@ -222,19 +314,20 @@ extern "C" kg_status kg_poisson_solve(int nx, int ny, int ns, const double* f, d
 			}
 			const int m = (int)std::min<long long>(opts->sweeps_per_check, opts->max_sweeps - sweeps);
 			if (ir) {
-				cudaMemsetAsync(e, 0, sizeof(float) * n, st);
+				cudaMemsetAsync(e, 0, sizeof(float) * ne, st);
 				if (jac) cudaMemsetAsync(e2, 0, sizeof(float) * n, st);
 				for (int it = 0; it < m; it++) {
 					if (jac) {
 						jacobi_kernel<<<gj.grid, gj.block, 0, st>>>(e, e2, r32, nx, ny, ns);
 						float* t = e; e = e2; e2 = t;
 					} else {
-						rb_sor_kernel<float><<<gp.grid, gp.block, 0, st>>>(e, r32, nx, ny, ns, (float)opts->omega, 0);
-						rb_sor_kernel<float><<<gp.grid, gp.block, 0, st>>>(e, r32, nx, ny, ns, (float)opts->omega, 1);
+						const float w = (float)opts->omega;
+						rb_sor_split_kernel<<<gs.grid, gs.block, 0, st>>>(e, e + half, r32, nx, ny, ns, nh, w, 0);
+						rb_sor_split_kernel<<<gs.grid, gs.block, 0, st>>>(e + half, e, r32 + half, nx, ny, ns, nh, w, 1);
 					}
 				}
 				const long long nb = std::min<long long>((n + 255) / 256, 152 * 16);
-				axpy_kernel<<<(unsigned)nb, 256, 0, st>>>(u, e, n);
+				axpy_kernel<<<(unsigned)nb, 256, 0, st>>>(u, e, nx, ny, ns, nh);
 				R.outer++;
 			} else {
 				for (int it = 0; it < m; it++) {
