@@ -444,8 +444,9 @@ int* tma_error_flag();
 long long tma_wait_limit();
 
 // Planes per run along z: z is split into runs so that the CTAs fill whole
-// waves of per_sm x sms, weighing each run's extra window planes.
-inline int tma_run_length(int per_sm, int sms, long long tiles, int dz, int nzmax)
+// waves of per_sm x sms, weighing each run's extra window planes (weight w
+// each) and a fixed cost per run.
+inline int tma_run_length(int per_sm, int sms, long long tiles, int dz, int nzmax, double w = 1.0, double fixed = 2.0)
 {
 	const long long slots = (long long)per_sm * sms;
 	int nz = 1;
@@ -454,7 +455,7 @@ inline int tma_run_length(int per_sm, int sms, long long tiles, int dz, int nzma
 		const long long ctas = tiles * c;
 		const double waves = (double)((ctas + slots - 1) / slots);
 		const int run = (dz + c - 1) / c;
-		const double cost = waves * (run + nzmax - 1 + 2);
+		const double cost = waves * (run + w * (nzmax - 1) + fixed);
 		if (cost < best * 0.999) { best = cost; nz = c; }
 	}
 	return (dz + nz - 1) / nz;

@@ -343,10 +343,16 @@ struct TmaVecLaunch {
 			const int gy = (dy + BY - 1) / BY;
 			// z split into runs so that the CTAs fill whole waves (all tiles
 			// then walk the same planes at about the same time, and the halo
-			// rows of neighbouring tiles are served from L2)
+			// rows of neighbouring tiles are served from L2).  Window planes
+			// weigh a quarter of a plane and a run nothing more: fitted to
+			// sweeps of fixed run counts on GB300 (Gpts/s, FP32 at 512x256x256
+			// and 1024x512x512, runs per tile 7-9 / 14 / 19 / 28): laplacian 657
+			// / 672 / 668 / 649 and 795 / 837 / 847 / 851, gradient 318 / 338 /
+			// 347 / 358 and 366 / 388 / 394 / 399, wave13pt (5-plane window)
+			// 486 / 442 / 429 / 408 and 559 / 553 / 539 / 516.
 			constexpr int zruns = KG_TMAVEC_ZRUNS > 0 ? KG_TMAVEC_ZRUNS : 1;
 			const int kc = KG_TMAVEC_ZRUNS > 0 ? (dz + zruns - 1) / zruns
-				: tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX());
+				: tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX(), 0.25, 0.0);
 			const int nz = (dz + kc - 1) / kc;
 			for (int y0 = 0; y0 < gy; y0 += 65535) {
 				dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
