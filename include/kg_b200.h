@@ -145,6 +145,16 @@ kg_status kg_matvec(kg_dtype dt, int nx, int ny,
 kg_status kg_matmul(kg_dtype dt, int nx, int ny, int ns,
 	const void* A, const void* B, void* C, kg_stream_t stream);
 
+/* The same C(i,j) += sum over k of A(i,k) B(k,j) on FP32 arrays (same
+ * layout) on the tensor cores: each operand split into a TF32 part and an
+ * exact FP32 remainder, three TF32 products per product (tcgen05 kind::tf32,
+ * FP32 accumulation), then added to C.  FP32-accurate (about 1e-7 of the sum
+ * of |A(i,k) B(k,j)|), not the k-ordered sum: not bit for bit with
+ * kg_matmul.  Takes a workspace of 8 (nx + ns) kp bytes (kp: ny rounded up
+ * to a multiple of 32) from the stream-ordered pool.  KG_ENOTSUP off Blackwell; a wait that gives up is
+ * reported by kg_engine_status. */
+kg_status kg_matmul_tc(int nx, int ny, int ns, const float* A, const float* B, float* C, kg_stream_t stream);
+
 /* sincos/sincos.F90:60-72: xy = sin(x) + cos(y) at every point (CUDA's
  * sin/cos: within 2 ulp of the correctly rounded values, not bitwise). */
 kg_status kg_sincos(kg_dtype dt, int nx, int ny, int ns,

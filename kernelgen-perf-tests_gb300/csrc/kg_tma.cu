@@ -58,6 +58,26 @@ cudaError_t tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, const void
 	return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// A rank-2 tiled map over an FP32 array of `outer` rows of `inner` elements
+// (rows contiguous, inner * 4 a multiple of 16 bytes) with boxes of
+// box_inner x box_outer elements in the 128-byte swizzle (box_inner * 4 <=
+// 128), zero fill outside the array.
+cudaError_t tma_encode_2d_sw128(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer, int box_inner,
+	int box_outer)
+{
+	cudaError_t e;
+	PFN_cuTensorMapEncodeTiled_v12000 encode = encode_fn(&e);
+	if (!encode) return e != cudaSuccess ? e : cudaErrorSymbolNotFound;
+	const cuuint64_t dims[2] = {inner, outer};
+	const cuuint64_t strides[1] = {inner * 4};
+	const cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_outer};
+	const cuuint32_t estr[2] = {1, 1};
+	CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+		CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+		CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 // The device address of g_tma_error on the current device, looked up once per
 // device and cached (it does not survive cudaDeviceReset).
 int* tma_error_flag()

@@ -10,7 +10,8 @@
  * the GPU through the kg_b200 C ABI.  The printed means are summed on the
  * host in the reference's order from the arrays copied back.
  *
- * Knobs: B200_PREC fp64 (default; strict IEEE) | fp64fma | fp32;
+ * Knobs: B200_PREC fp64 (default; strict IEEE) | fp64fma | fp32 | fp32tc
+ *        (matmul only: FP32 arrays on the tensor cores, kg_matmul_tc);
  *        NO_TIMING, PROFILING_FNAME as in the reference.
  * "<name> kernel time = t" is, as the reference's launch interposer prints
  * it (cuda_profiling.cu:239-249), host wall time from before the launch to
@@ -58,12 +59,14 @@ static int parse_arg(const char* name, const char* arg)
 	return v;
 }
 
+static int g_tc;   /* B200_PREC=fp32tc */
 static kg_dtype parse_prec(const char* s)
 {
 	if (!s || !*s || !strcmp(s, "fp64")) return KG_F64;
 	if (!strcmp(s, "fp64fma")) return KG_F64_FMA;
 	if (!strcmp(s, "fp32")) return KG_F32;
-	fprintf(stderr, "Unknown B200_PREC=%s (fp64 | fp64fma | fp32)\n", s);
+	if (!strcmp(s, "fp32tc")) { g_tc = 1; return KG_F32; }
+	fprintf(stderr, "Unknown B200_PREC=%s (fp64 | fp64fma | fp32 | fp32tc)\n", s);
 	exit(1);
 }
 
@@ -95,6 +98,7 @@ int main(int argc, char* argv[])
 	const char* prof_name = getenv("PROFILING_FNAME");
 	const kg_dtype dt = parse_prec(getenv("B200_PREC"));
 	const size_t es = dt == KG_F32 ? 4 : 8;
+	if (g_tc && test != T_MATMUL) { fprintf(stderr, "B200_PREC=fp32tc is for matmul only\n"); return 1; }
 
 	const int nx = parse_arg("nx", argv[1]);
 	const int ny = parse_arg("ny", argv[2]);
@@ -218,7 +222,10 @@ int main(int argc, char* argv[])
 		case T_VECADD: KG_CHECK(kg_vecadd(dt, nx, ny, ns, p[0], p[1], p[2], 0)); break;
 		case T_SINCOS: KG_CHECK(kg_sincos(dt, nx, ny, ns, p[0], p[1], p[2], 0)); break;
 		case T_MATVEC: KG_CHECK(kg_matvec(dt, nx, ny, p[0], p[1], p[2], 0)); break;
-		case T_MATMUL: KG_CHECK(kg_matmul(dt, nx, ny, ns, p[0], p[1], p[2], 0)); break;
+		case T_MATMUL:
+			if (g_tc) KG_CHECK(kg_matmul_tc(nx, ny, ns, (const float*)p[0], (const float*)p[1], (float*)p[2], 0));
+			else KG_CHECK(kg_matmul(dt, nx, ny, ns, p[0], p[1], p[2], 0));
+			break;
 		case T_WHISPERING:
 			KG_CHECK(kg_whispering(dt, nx, ny, mu, epsilon, p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], 0));
 			break;
@@ -237,6 +244,8 @@ int main(int argc, char* argv[])
 	CU_CHECK(cudaDeviceSynchronize());
 	kgh_get_time(&t1);
 	const double compute_t = kgh_time_diff(&t0, &t1);
+	/* a tensor-core matmul whose bounded wait gave up left C incomplete */
+	if (g_tc) KG_CHECK(kg_engine_status(0));
 	if (prof_name)
 		for (int it = 0; it < nt; it++) {
 			float ms = 0;

@@ -38,7 +38,7 @@ EXPORTS = [
     "kg_batch_create", "kg_batch_step", "kg_batch_capture", "kg_batch_launch", "kg_batch_tune",
     "kg_batch_set_config", "kg_batch_get_config", "kg_batch_set_step", "kg_batch_final_roles",
     "kg_batch_destroy", "kg_poisson_solve", "kg_engine_status",
-    "kg_vecadd", "kg_matvec", "kg_matmul", "kg_sincos", "kg_whispering", "kg_extra_regcount",
+    "kg_vecadd", "kg_matvec", "kg_matmul", "kg_matmul_tc", "kg_sincos", "kg_whispering", "kg_extra_regcount",
     "kg_plan_kernels", "kg_exact_arith", "kg_set_tma_wait_limit",
 ]
 EXTRA_TESTS = ["vecadd", "matvec", "matmul", "sincos", "whispering"]
@@ -126,6 +126,7 @@ def _sig(lib):
         "kg_vecadd": [I, I, I, I, P, P, P, P],
         "kg_matvec": [I, I, I, P, P, P, P],
         "kg_matmul": [I, I, I, I, P, P, P, P],
+        "kg_matmul_tc": [I, I, I, P, P, P, P],
         "kg_sincos": [I, I, I, I, P, P, P, P],
         "kg_whispering": [I, I, I, D, D] + [P] * 9 + [P],
         "kg_extra_regcount": [ctypes.c_char_p, I, ctypes.POINTER(I)],
