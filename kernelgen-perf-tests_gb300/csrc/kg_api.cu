@@ -95,8 +95,6 @@ static kg_status validate(const kg_problem* p)
 	if (p->engine != KG_ENGINE_AUTO && !((engines_built(p->dtype) >> p->engine) & 1))
 		return fail(KG_ENOTSUP, "%s: engine %d is not built for dtype %d", m.name, p->engine, p->dtype);
 	if (m.is2d && p->ns != 1) return fail(KG_EINVAL, "%s: 2D stencil needs ns == 1", m.name);
-	if (p->engine == KG_ENGINE_TMA_VEC && m.is2d)
-		return fail(KG_ENOTSUP, "%s: the vector TMA engine is built for 3D stencils", m.name);
 	const size_t n = (size_t)p->nx * (size_t)p->ny * (size_t)p->ns;
 	if (n == 0) return KG_OK;
 	if (n > ((size_t)1 << 40)) return fail(KG_EINVAL, "%s: %zu points is beyond the supported size", m.name, n);

@@ -152,6 +152,7 @@ struct TMaps {
 constexpr int pow2_at_least(int n) { int p = 1; while (p < n) p *= 2; return p; }
 
 template <class Op, class S, int BX, int BY, int L> struct TGeo {
+	static constexpr int kBY = BY;
 	static constexpr int ES = (int)sizeof(S);
 	static constexpr int A = 16 / ES;                       // x alignment, elements
 	static constexpr int NIN = Op::slots().nin;
@@ -216,7 +217,9 @@ template <class Op, class N, class S, class G, int ZMAX> struct TAcc {
 
 // ---- kernel -------------------------------------------------------------
 
-template <class Op, class S, class G>
+// BAND: a 2D op walked in bands of BY rows (step k = band k, rows yt + k BY
+// onward; the arrays' maps are rank 3 with one plane).
+template <class Op, class S, class G, bool BAND = false>
 __device__ __forceinline__ void tma_issue(const TMaps& maps, unsigned char* sm, uint64_t* bar,
 	int xt, int yt, int k, bool window)
 {
@@ -227,8 +230,12 @@ __device__ __forceinline__ void tma_issue(const TMaps& maps, unsigned char* sm, 
 		const Halo h = Op::halo(q);
 		const int x = xt - G::XL(q), y = yt - h.y0;
 		const int p1 = k + h.z1;
-		for (int p = window ? k - h.z0 : p1; p <= p1; p++)
-			tma_load_3d(sm + G::offset(q) + G::slot(q, p) * G::PS(q), &maps.m[q], bar, x, y, p);
+		for (int p = window ? k - h.z0 : p1; p <= p1; p++) {
+			if constexpr (BAND)
+				tma_load_3d(sm + G::offset(q) + G::slot(q, p) * G::PS(q), &maps.m[q], bar, x, y + p * G::kBY, 0);
+			else
+				tma_load_3d(sm + G::offset(q) + G::slot(q, p) * G::PS(q), &maps.m[q], bar, x, y, p);
+		}
 	}
 }
 
@@ -248,6 +255,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 // The runs of one CTA of the TMA engine: planes kb, kb + gridDim.z kc, ...
 // (up to kc each) of its tile (xt, yt).
 struct ZRuns {
+	static constexpr bool kBand = false;
 	int xt, yt, kb, kend, kc;
 	__device__ __forceinline__ bool next(int& x, int& y, int& k0, int& n) {
 		if (kb >= kend) return false;
@@ -258,6 +266,12 @@ struct ZRuns {
 		kb += gridDim.z * kc;
 		return true;
 	}
+};
+
+// The same runs over the bands of BY rows of a 2D op (band k: rows
+// yt + k BY ...; the producer's copies then start at row yt + k BY - y0).
+struct BandRuns : ZRuns {
+	static constexpr bool kBand = true;
 };
 
 template <class Op, class S, class G, class Runs>
@@ -279,7 +293,7 @@ __device__ __forceinline__ void tma_produce(const TMaps& maps, unsigned char* sm
 			if (t >= L + 1) ok = mbar_wait(&done[(gt - L - 1) % NB], ((gt - L - 1) / NB) & 1, kTmaWaitCycles, abort);
 			if (!ok) break;
 			fence_proxy_async();
-			tma_issue<Op, S, G>(maps, sm, &full[gt % NB], xt, yt, kb + t, t == 0);
+			tma_issue<Op, S, G, Runs::kBand>(maps, sm, &full[gt % NB], xt, yt, kb + t, t == 0);
 			issued = gt + 1;
 		}
 		g += nsteps;

@@ -12,8 +12,11 @@
 // 7-point body costs about 7 vector loads per V points instead of 7 scalar
 // loads per point, and the outputs leave as one vector store per row.
 //
-// For 3D ops with storage of 4 or 2 bytes (FP32, BF16, FP16; FP32
-// arithmetic) whose reach along x is at most V on either side.
+// For ops with storage of 4 or 2 bytes (FP32, BF16, FP16; FP32 arithmetic)
+// whose reach along x is at most V on either side.  3D ops stream along z;
+// 2D ops stream down bands of BY rows: step k is the band of rows LY + k BY
+// onward, its box grown by the op's reach in y (re-read from L2 by the
+// neighbouring band), the arrays' tensor maps rank 3 with one plane.
 #pragma once
 
 #include <algorithm>
@@ -133,11 +136,20 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	uint64_t* done = full + NB;
 	volatile int* abort = reinterpret_cast<volatile int*>(sm + G::kAbort);
 
+	// 2D ops walk bands of BY rows instead of planes: step k covers rows
+	// LY + k BY ... (one tile column per CTA in y)
+	constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
 	const int tid = threadIdx.x;
 	const int xt = blockIdx.x * BX, yt = Op::LY + (yt0 + (int)blockIdx.y) * BY;
-	const int kend = ns - Op::HZ;
-	// the CTA's runs along z (each run is a window plus steps of planes)
-	const ZRuns runs{xt, yt, Op::LZ + (int)blockIdx.z * kc, kend, kc};
+	const int kend = k2d ? (ny - Op::LY - Op::HY + BY - 1) / BY : ns - Op::HZ;
+	// the CTA's runs along z or down the bands (each run is a window plus steps)
+	using Runs = std::conditional_t<k2d, BandRuns, ZRuns>;
+	Runs runs;
+	runs.xt = xt;
+	runs.yt = yt;
+	runs.kb = Op::LZ + (int)blockIdx.z * kc;
+	runs.kend = kend;
+	runs.kc = kc;
 
 	if (tid == 0) {
 		for (int b = 0; b < NB; b++) {
@@ -157,7 +169,7 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	// ---- compute warps ----
 	const int lane = tid & 31, w = tid >> 5;
 	const int lx = lane % LPR, ry = w * RPW + lane / LPR;
-	const long long sy = nx, sz = (long long)nx * ny;
+	const long long sy = nx, sz = k2d ? (long long)nx * BY : (long long)nx * ny;
 	// byte offset of the lane's first column in the point's row of a plane, per input
 	int toff[6];
 #pragma unroll
@@ -165,20 +177,22 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 		toff[q] = ((ry + Op::halo(q).y0) * G::W(q) + lx * V + G::XL(q)) * G::ES;
 
 	const int i0 = xt + lx * V, j = yt + ry;
+	unsigned cols = 0;
+#pragma unroll
+	for (int v = 0; v < V; v++)
+		if (i0 + v >= Op::LX && i0 + v < nx - Op::HX) cols |= 1u << v;
+	// rows in the domain: fixed for 3D ops, per band for 2D ones
+	auto rows_valid = [&](int band, unsigned (&valid)[PY]) {
+#pragma unroll
+		for (int r = 0; r < PY; r++) valid[r] = j + r * RB + band * BY < ny - Op::HY ? cols : 0u;
+	};
 	unsigned valid[PY];
-#pragma unroll
-	for (int r = 0; r < PY; r++) {
-		const bool row_ok = j + r * RB < ny - Op::HY;
-		valid[r] = 0;
-#pragma unroll
-		for (int v = 0; v < V; v++)
-			if (row_ok && i0 + v >= Op::LX && i0 + v < nx - Op::HX) valid[r] |= 1u << v;
-	}
+	rows_valid(0, valid);
 	// step counters kept incrementally: barrier index and phase of the step,
 	// and the ring slot of the step's plane of every input
 	int bi = 0;
 	uint32_t ph = 0;
-	ZRuns rz = runs;
+	Runs rz = runs;
 	int xr, yr, kb, nsteps;
 	while (rz.next(xr, yr, kb, nsteps)) {
 		int s0[6];
@@ -186,6 +200,7 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 		for (int q = 0; q < G::NIN; q++) s0[q] = G::slot(q, kb);
 		const long long c0 = i0 + sy * j + sz * kb;
 		for (int s = 0; s < nsteps; s++) {
+			if (k2d) rows_valid(kb + s, valid);
 			const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[bi], ph, wait, abort));
 			if (!ok) {
 				if (lane == 0) {
@@ -280,8 +295,9 @@ struct TmaVecLaunch {
 			if (Op::halo(q).x0 > V || Op::halo(q).x1 > V) return false;
 		return true;
 	}
-	// built for 3D ops on 4- and 2-byte storage whose reach along x fits
-	static constexpr bool built = !k2d && (sizeof(S) == 4 || sizeof(S) == 2) && reach_ok();
+	// built for 4- and 2-byte storage where the reach along x fits (3D ops
+	// along z, 2D ops down bands of BY rows)
+	static constexpr bool built = (sizeof(S) == 4 || sizeof(S) == 2) && reach_ok();
 	static const void* func() {
 		if constexpr (built) return (const void*)tma_vec_kernel<Op, N, S, V, NW, PY, L>;
 		else return nullptr;
@@ -309,8 +325,10 @@ struct TmaVecLaunch {
 			for (int q = 0; q < sl.nin; q++) p.in[q] = (const S*)pr.arr[sl.in[q]];
 			for (int q = 0; q < sl.nout; q++) p.out[q] = (S*)pr.arr[sl.out[q]];
 			const int nx = pr.nx, ny = pr.ny, ns = pr.ns;
-			const int dx = nx - Op::LX - Op::HX, dy = ny - Op::LY - Op::HY, dz = ns - Op::LZ - Op::HZ;
-			if (dx <= 0 || dy <= 0 || dz <= 0) return cudaSuccess;
+			const int dx = nx - Op::LX - Op::HX, dy = ny - Op::LY - Op::HY;
+			if (dx <= 0 || dy <= 0 || ns - Op::LZ - Op::HZ <= 0) return cudaSuccess;
+			// 2D: one tile column in y, the bands of BY rows as the steps
+			const int dz = k2d ? (dy + BY - 1) / BY : ns - Op::LZ - Op::HZ;
 			constexpr size_t smem = G::total();
 			static std::atomic<int> occ_of[64];
 			int dev = 0;
@@ -340,7 +358,7 @@ struct TmaVecLaunch {
 				if (e != cudaSuccess) return e;
 			}
 			const int gx = (nx - Op::HX + BX - 1) / BX;
-			const int gy = (dy + BY - 1) / BY;
+			const int gy = k2d ? 1 : (dy + BY - 1) / BY;
 			// z split into runs so that the CTAs fill whole waves (all tiles
 			// then walk the same planes at about the same time, and the halo
 			// rows of neighbouring tiles are served from L2).  Window planes
