@@ -50,7 +50,8 @@ typedef enum {
 	KG_F32 = 2,      /* FP32 storage and arithmetic                           */
 	KG_BF16 = 3,     /* BF16 storage, FP32 arithmetic                         */
 	KG_F16 = 4,      /* FP16 storage, FP32 arithmetic                         */
-	KG_U8 = 5,       /* 0/1 byte cells: gameoflife only (B3/S23)              */
+	KG_U8 = 5,       /* 0/1 byte cells: gameoflife only (B3/S23; other byte
+	                    values give unspecified cells)                       */
 	KG_F64_FF = 6,   /* FP64 storage; arithmetic on float-float pairs (hi+lo
 	                    FP32 with error-free transformations) on the FP32 pipes:
 	                    ~1e-14 of FP64 normwise, values within FP32's range    */

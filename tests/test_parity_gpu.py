@@ -141,7 +141,10 @@ def test_narrow_storage_error_bounds(name, dtype):
             name, q, err, TOL[dtype], out_slots)
 
 
-@pytest.mark.parametrize("shape", [(3, 3), (5, 7), (67, 45), (512, 1031)])
+# rows of a multiple of 16 bytes take the 16-cell vector kernel: one vector a
+# row (both rims in it), a partial warp, two warps a row, one interior row
+@pytest.mark.parametrize("shape", [(3, 3), (5, 7), (67, 45), (512, 1031), (16, 40), (48, 33), (1024, 100),
+                                   (32, 3)])
 def test_conway_u8_bitwise(shape):
     nx, ny = shape
     b0, b1 = ol.bernoulli_u8(nx * ny)
@@ -157,10 +160,11 @@ def test_conway_u8_bitwise(shape):
     assert np.array_equal(by[ptrs[1]].cpu().numpy(), b1)
 
 
-def test_conway_u8_equals_fp64_reference_rule():
+@pytest.mark.parametrize("shape", [(130, 77), (128, 77)])
+def test_conway_u8_equals_fp64_reference_rule(shape):
     """Bernoulli(0.3) cells: the FP64 sweep (the reference rule) thresholded
-    at 0.5 equals the byte sweep, sweep after sweep."""
-    shape = (130, 77)
+    at 0.5 equals the byte sweep, sweep after sweep (scalar and vector
+    kernels)."""
     case = ol.Case("gameoflife", shape, variant=ol.INIT_BERNOULLI)
     f = gpu_run("gameoflife", kgb200.KG_F64, case.shape, [], case.arrays(), 9)
     b0, b1 = (x.astype(np.uint8) for x in case.arrays())
