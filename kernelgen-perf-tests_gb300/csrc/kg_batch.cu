@@ -486,7 +486,13 @@ __global__ void batch_rim_copy(const BatchDesc* __restrict__ desc, int nprob, in
 // reads its inputs from global memory instead (the last up to 15 bytes of an
 // array).  Every point is the same body as the other engines evaluate.
 
-constexpr int kBulkL = 3;              // steps of copies in flight
+// Steps of copies in flight.  Measured on the 256-problem FP32 batch: 2
+// steps make the rings small enough for 3 resident CTAs per SM, but the best
+// configuration is no faster (394 against 396 Gpts/s).
+#ifndef KG_BULK_L
+#define KG_BULK_L 3
+#endif
+constexpr int kBulkL = KG_BULK_L;
 constexpr int kBulkNB = kBulkL + 1;    // mbarriers per direction
 constexpr int kBulkBar = 128;          // bytes: 2 x kBulkNB mbarriers, the abort flag
 
