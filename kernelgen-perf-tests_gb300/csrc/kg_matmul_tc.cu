@@ -32,6 +32,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "kg_internal.h"
 #include "kg_tma.cuh"
@@ -357,8 +358,15 @@ extern "C" kg_status kg_matmul_tc(int nx, int ny, int ns, const float* A, const 
 	if (e == cudaSuccess) {
 		auto launch = [&](auto shape) {
 			using T = decltype(shape);
-			cudaError_t r = cudaFuncSetAttribute(matmul_tc_kernel<T::N>, cudaFuncAttributeMaxDynamicSharedMemorySize, T::Smem);
-			if (r != cudaSuccess) return r;
+			// the shared-memory opt-in, once per device
+			static std::atomic<bool> set[64];
+			if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+			if (!set[dev].load(std::memory_order_acquire)) {
+				cudaError_t r = cudaFuncSetAttribute(matmul_tc_kernel<T::N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+					T::Smem);
+				if (r != cudaSuccess) return r;
+				set[dev].store(true, std::memory_order_release);
+			}
 			dim3 grid((unsigned)((nx + kTcM - 1) / kTcM), (unsigned)((ns + T::N - 1) / T::N));
 			matmul_tc_kernel<T::N><<<grid, 128, T::Smem, st>>>(maps[0], maps[1], maps[2], maps[3], C, nx, ns, kp / kTcK,
 				err, tma_wait_limit());

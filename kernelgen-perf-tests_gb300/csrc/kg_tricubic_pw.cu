@@ -39,7 +39,9 @@ constexpr int kTriPwEmu = KG_PW_EMU;
 // kTriPwAddInt of every run of 16 terms (one kk).  Measured (ms per sweep,
 // tricubic / tricubic2, products on the integer pipes 3 of 4): 0 additions
 // 5.686 / 5.824, 1: 5.652 / 5.698, 2: 5.787 / 5.780; with 2 of 4 products
-// and 2 or 4 additions 6.104 / 6.272 and 5.822 / 5.903.
+// and 2 or 4 additions 6.104 / 6.272 and 5.822 / 5.903; with all 4 products
+// and 0 or 1 addition (ms per 10-sweep program, weights included) 61.5 /
+// 61.0 and 63.9 / 63.4 against 56.1 / 56.7.
 constexpr int kTriPwAddInt = KG_PW_ADD_INT;
 
 constexpr int kPwBX = 32, kPwBY = 8, kPwKC = 8;
