@@ -140,6 +140,52 @@ __global__ void __launch_bounds__(kSX * kSY) jacobi_kernel(const float* __restri
 	}
 }
 
+// The same sweep with a lane on 4 consecutive points of a row as 16-byte
+// vectors (rows of a multiple of 4 elements, 16-byte aligned arrays): the x
+// neighbours outside the vector come from the neighbouring lanes by warp
+// shuffles (the warp's end lanes load theirs).  The outer planes of e1 stay
+// 0 (positions 0 and nx - 1 of a row are written as 0, their value).  Same
+// operands, order and expression as jacobi_kernel.
+__global__ void __launch_bounds__(kSX * kSY) jacobi_vec_kernel(const float* __restrict__ e0, float* __restrict__ e1,
+	const float* __restrict__ rhs, int nx, int ny, int ns)
+{
+	const long long sy = nx, sz = (long long)nx * ny;
+	const int lane = threadIdx.x;
+	const int i0 = (blockIdx.x * kSX + lane) * kSV;
+	const bool inrow = i0 < nx;
+	auto ld = [](const float* q) { return __ldg(reinterpret_cast<const float4*>(q)); };
+	for (int k = 1 + blockIdx.z; k < ns - 1; k += gridDim.z) {
+		for (int j = 1 + blockIdx.y * kSY + threadIdx.y; j < ny - 1; j += gridDim.y * kSY) {
+			const long long c = i0 + sy * j + sz * k;
+			float4 m = make_float4(0.f, 0.f, 0.f, 0.f), ym = m, yp = m, zm = m, zp = m, r = m;
+			if (inrow) {
+				m = ld(e0 + c);
+				ym = ld(e0 + c - sy);
+				yp = ld(e0 + c + sy);
+				zm = ld(e0 + c - sz);
+				zp = ld(e0 + c + sz);
+				r = ld(rhs + c);
+			}
+			float left = __shfl_up_sync(0xffffffffu, m.w, 1), right = __shfl_down_sync(0xffffffffu, m.x, 1);
+			if (lane == 0 && inrow && i0 > 0) left = __ldg(e0 + c - 1);
+			if (lane == kSX - 1 && inrow && i0 + kSV < nx) right = __ldg(e0 + c + kSV);
+			if (!inrow) continue;
+			const float xl[kSV] = {left, m.x, m.y, m.z}, xr[kSV] = {m.y, m.z, m.w, right};
+			const float y0[kSV] = {ym.x, ym.y, ym.z, ym.w}, y1[kSV] = {yp.x, yp.y, yp.z, yp.w};
+			const float z0[kSV] = {zm.x, zm.y, zm.z, zm.w}, z1[kSV] = {zp.x, zp.y, zp.z, zp.w};
+			const float rr[kSV] = {r.x, r.y, r.z, r.w};
+			float o[kSV];
+#pragma unroll
+			for (int v = 0; v < kSV; v++) {
+				const int i = i0 + v;
+				const float s = xl[v] + xr[v] + y0[v] + y1[v] + z0[v] + z1[v];
+				o[v] = (i > 0 && i < nx - 1) ? (s + rr[v]) * (1.0f / 6.0f) : 0.0f;
+			}
+			*reinterpret_cast<float4*>(e1 + c) = make_float4(o[0], o[1], o[2], o[3]);
+		}
+	}
+}
+
 // r = f - A u on the interior (FP64); r32 = (float) r (0 on the outer
 // planes), interleaved (nh = 0) or split by colour (rows of nh elements);
 // partial[b] = this block's sum of r^2.
@@ -289,6 +335,11 @@ extern "C" kg_status kg_poisson_solve(int nx, int ny, int ns, const double* f, d
 		const double fnorm = std::sqrt(host[0]);
 		R.fnorm = fnorm;
 		const Grid3 gp = sweep_grid(nx, ny, ns, true), gj = sweep_grid(nx, ny, ns, false);
+		// Jacobi sweeps on 16-byte vectors where rows allow them (the work
+		// arrays come from cudaMallocAsync: 256-byte aligned)
+		const bool jvec = nx % kSV == 0;
+		Grid3 gv = sweep_grid(nx, ny, ns, false);
+		gv.grid.x = (unsigned)std::max(1, (nx + kSX * kSV - 1) / (kSX * kSV));
 		Grid3 gs = sweep_grid(nx, ny, ns, true);
 		gs.grid.x = (unsigned)std::max(1, (nh + kSX * kSV - 1) / (kSX * kSV));
 		long long sweeps = 0;
@@ -318,7 +369,8 @@ extern "C" kg_status kg_poisson_solve(int nx, int ny, int ns, const double* f, d
 				if (jac) cudaMemsetAsync(e2, 0, sizeof(float) * n, st);
 				for (int it = 0; it < m; it++) {
 					if (jac) {
-						jacobi_kernel<<<gj.grid, gj.block, 0, st>>>(e, e2, r32, nx, ny, ns);
+						if (jvec) jacobi_vec_kernel<<<gv.grid, gv.block, 0, st>>>(e, e2, r32, nx, ny, ns);
+						else jacobi_kernel<<<gj.grid, gj.block, 0, st>>>(e, e2, r32, nx, ny, ns);
 						float* t = e; e = e2; e2 = t;
 					} else {
 						const float w = (float)opts->omega;

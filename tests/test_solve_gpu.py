@@ -100,6 +100,38 @@ def test_refinement_sweeps_match_fp32_restatement(shape):
     assert np.max(np.abs(u - e.astype(np.float64))) <= 1e-5 * max(np.max(np.abs(e)), 1e-30)
 
 
+def fp32_jacobi(r, shape, sweeps):
+    """FP32 Jacobi sweeps on A e = r from e = 0 (numpy float32, the GPU
+    sweep's operand order); returns e."""
+    nx, ny, ns = shape
+    rr = r.reshape(ns, ny, nx)
+    e = np.zeros((ns, ny, nx), np.float32)
+    sixth = np.float32(1.0 / 6.0)
+    for _ in range(sweeps):
+        n = np.zeros_like(e)
+        s = (((((e[1:-1, 1:-1, :-2] + e[1:-1, 1:-1, 2:]) + e[1:-1, :-2, 1:-1]) + e[1:-1, 2:, 1:-1]) +
+              e[:-2, 1:-1, 1:-1]) + e[2:, 1:-1, 1:-1])
+        n[1:-1, 1:-1, 1:-1] = (s + rr[1:-1, 1:-1, 1:-1]) * sixth
+        e = n
+    return e.reshape(-1)
+
+
+@pytest.mark.parametrize("shape", [(20, 17, 15), (21, 18, 16), (136, 9, 7)])
+def test_jacobi_refinement_sweeps_match_fp32_restatement(shape):
+    """One outer step of refinement around FP32 Jacobi sweeps from u = 0
+    (16-byte vectors with shuffled x neighbours where nx is a multiple of 4):
+    bit for bit the FP32 restatement (no product to contract)."""
+    m = 5
+    f = poisson_rhs(shape)
+    fd = torch.from_numpy(f).cuda()
+    ud = torch.zeros_like(fd)
+    st, rep = kgb200.poisson_solve(shape, fd.data_ptr(), ud.data_ptr(), kgb200.KG_SOLVE_IR_JACOBI_F32,
+                                   rtol=1e-30, sweeps_per_check=m, max_sweeps=m, raise_on_timeout=False)
+    assert st == 4 and rep.sweeps == m and rep.outer == 1
+    e = fp32_jacobi(f.astype(np.float32), shape, m)
+    assert np.array_equal(ud.cpu().numpy(), e.astype(np.float64))
+
+
 def test_refinement_keeps_the_sor_rate():
     """Refinement with FP32 inner SOR needs about as many sweeps as FP64 SOR."""
     shape = (48, 40, 32)
