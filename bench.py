@@ -947,8 +947,61 @@ def run_other(reps=10):
         row["cpu_oracle_ms_per_step"] = round(max((t1 - t0) - (t2 - t1), 1e-9) * 1e3, 2)
         row["speedup_f64_vs_cpu"] = round(row["cpu_oracle_ms_per_step"] / row["f64"]["ms_per_step"], 1)
         out[name] = row
+    out["matmul_tc"] = run_matmul_tc()
     out["note"] = ("one step at the suite's problem size; KG_F64 bitwise equal to the oracle; CPU: the oracle's "
                    "fast-math build on the host cores (step time = program time minus its init)")
+    return out
+
+
+def run_matmul_tc(sizes=((512, 256, 256), (4096, 4096, 4096)), reps=5):
+    """kg_matmul_tc (FP32 arrays on the tensor cores, three TF32 MMAs per
+    product) at the suite's size and at 4096^3, beside kg_matmul's FP32 SIMT
+    kernel at the suite's size; FP32-accurate TFLOP/s count 2 nx ny ns, the
+    TF32 MMA rate three times that, against half the measured dense BF16
+    rate (the TF32 tensor rate)."""
+    import torch
+
+    lib = kgb200.load()
+    bf16 = None
+    try:
+        with open(PEAKS_FILE) as f:
+            bf16 = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        pass
+    out = {}
+    for nx, ny, ns in sizes:
+        g = torch.Generator(device="cuda")
+        g.manual_seed(nx + ny + ns)
+        A = torch.rand(nx * ny, generator=g, device="cuda") * 2 - 1
+        B = torch.rand(ny * ns, generator=g, device="cuda") * 2 - 1
+        C = torch.zeros(nx * ns, device="cuda")
+        calls = {"tc": lambda: lib.kg_matmul_tc(nx, ny, ns, A.data_ptr(), B.data_ptr(), C.data_ptr(), None)}
+        if nx * ny * ns <= 512 * 256 * 256:
+            calls["simt_f32"] = lambda: lib.kg_matmul(kgb200.KG_F32, nx, ny, ns, A.data_ptr(), B.data_ptr(),
+                                                       C.data_ptr(), None)
+        row = {}
+        for key, f in calls.items():
+            for _ in range(2):
+                kgb200.check(f())
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                kgb200.check(f())
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            flops = 2.0 * nx * ny * ns
+            r = {"ms": round(ms, 4), "tflops_fp32_accurate": round(flops / ms / 1e9, 1)}
+            if key == "tc":
+                r["tf32_mma_tflops"] = round(3 * flops / ms / 1e9, 1)
+                if bf16:
+                    r["tf32_frac_of_half_measured_bf16"] = round(3 * flops / ms / 1e9 / (bf16 / 2), 3)
+            row[key] = r
+        kgb200.engine_status()
+        out["x".join(map(str, (nx, ny, ns)))] = row
+        del A, B, C
+        torch.cuda.empty_cache()
     return out
 
 

@@ -42,6 +42,9 @@ namespace kg {
 // Tiles of 128 x TN (TN = 128: 3 stages of 64 KB; TN = 256 would take 2
 // stages of 96 KB).
 constexpr int kTcM = 128, kTcK = 32;
+#ifndef KG_TC_GROUP
+#define KG_TC_GROUP 8
+#endif
 constexpr int kTcBoxA = kTcM * kTcK * 4;              // bytes of one split of A
 template <int TN> struct TcShape {
 	static constexpr int N = TN;
@@ -201,7 +204,19 @@ __global__ void __launch_bounds__(128, 1) matmul_tc_kernel(const __grid_constant
 	uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
 	volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);   // the MMA issuer gave up
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int m0 = blockIdx.x * kTcM, n0 = blockIdx.y * kTcN;
+	// tile order: groups of KG_TC_GROUP row tiles, each walked column tile
+	// by column tile, so that the CTAs resident together share their A and B
+	// panels in L2 (the launch order is blockIdx.x fastest)
+	int mt_i, nt_i;
+	{
+		const int mt = (int)gridDim.x, nt = (int)gridDim.y;
+		const int b = (int)blockIdx.x + mt * (int)blockIdx.y;
+		const int per = KG_TC_GROUP * nt, g = b / per;
+		const int gm = min(KG_TC_GROUP, mt - g * KG_TC_GROUP), r = b - g * per;
+		mt_i = g * KG_TC_GROUP + r % gm;
+		nt_i = r / gm;
+	}
+	const int m0 = mt_i * kTcM, n0 = nt_i * kTcN;
 
 	if (threadIdx.x == 0) {
 		for (int s = 0; s < kTcStages; s++) {
