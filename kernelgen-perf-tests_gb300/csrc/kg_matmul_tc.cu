@@ -206,7 +206,9 @@ __global__ void __launch_bounds__(128, 1) matmul_tc_kernel(const __grid_constant
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	// tile order: groups of KG_TC_GROUP row tiles, each walked column tile
 	// by column tile, so that the CTAs resident together share their A and B
-	// panels in L2 (the launch order is blockIdx.x fastest)
+	// panels in L2 (the launch order is blockIdx.x fastest).  Measured: 8192^3
+	// 5.95 ms in row-major order, 5.79 in groups of 8 or 16; 4096^3 within 0.3 %.
+	// The kernel is not bound by DRAM misses but by its stages in flight.
 	int mt_i, nt_i;
 	{
 		const int mt = (int)gridDim.x, nt = (int)gridDim.y;
