@@ -174,25 +174,29 @@ kg_status kg_extra_regcount(const char* name, kg_dtype dt, int* nregs);
 
 /* ---- table-driven form of the same entry points ------------------------ */
 
-/* Which kernel design runs a sweep (kg_problem.engine).  AUTO: TMA for
- * KG_F32/KG_BF16/KG_F16 laplacian, divergence, gradient, uxx1 and lapgsrb
- * (and KG_F32 wave13pt) where every array and row starts on a 16-byte
- * boundary, else DIRECT; DIRECT for KG_F64/KG_F64_FMA; STAGED for KG_F64_FF
- * (TMA for its divergence and uxx1 where aligned).  Built: DIRECT and TMA
- * for every floating type but KG_F64_FF and KG_F64_MIX; STAGED and TMA for
- * KG_F64_FF; DIRECT for KG_F64_MIX and KG_U8.  Grids of tiles beyond the launch
- * limits are taken in turn.  The engines evaluate the same expressions in the
- * same order (the
- * tests check their outputs equal bit for bit).  TMA needs 16-byte aligned
- * arrays and rows. */
+/* Which kernel design runs a sweep (kg_problem.engine).  AUTO: TMA_VEC for
+ * KG_F32/KG_BF16/KG_F16 laplacian, divergence, gradient, uxx1, lapgsrb,
+ * wave13pt, jacobi, gaussblur and gameoflife where every array and row
+ * starts on a 16-byte boundary (TMA or DIRECT otherwise); DIRECT for
+ * KG_F64/KG_F64_FMA; STAGED for KG_F64_FF (TMA for its divergence and uxx1
+ * where aligned).  Built: DIRECT and TMA for every floating type but
+ * KG_F64_FF and KG_F64_MIX; TMA_VEC for KG_F32/KG_BF16/KG_F16; STAGED and TMA
+ * for KG_F64_FF; DIRECT for KG_F64_MIX and KG_U8.  Grids of tiles beyond the
+ * launch limits are taken in turn.  The engines evaluate the same
+ * expressions in the same order (the tests check their outputs equal bit for
+ * bit).  TMA and TMA_VEC need 16-byte aligned arrays and rows; TMA_VEC
+ * sweeps are launched as programmatic dependents of the kernel before them
+ * on the stream (their launch overlaps its tail; they read and write nothing
+ * before it has completed). */
 typedef enum {
 	KG_ENGINE_AUTO = 0,
 	KG_ENGINE_DIRECT = 1,   /* one thread per column, neighbours through L1     */
 	KG_ENGINE_STAGED = 2,   /* halo planes in shared memory, loaded by threads  */
 	KG_ENGINE_TMA = 3,      /* halo planes in shared memory by tiled bulk copy  */
-	KG_ENGINE_TMA_VEC = 4   /* the same copies; each thread evaluates 4
-	                           consecutive points from vector reads (3D ops,
-	                           FP32 arithmetic: KG_F32, KG_BF16, KG_F16)     */
+	KG_ENGINE_TMA_VEC = 4   /* the same copies; each thread evaluates 4 (8)
+	                           consecutive points from vector reads (3D ops
+	                           along z, 2D ops down bands of rows; FP32
+	                           arithmetic: KG_F32, KG_BF16, KG_F16)          */
 } kg_engine;
 
 typedef struct {
