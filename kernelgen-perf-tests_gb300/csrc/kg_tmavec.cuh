@@ -20,6 +20,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "kg_tma.cuh"
@@ -32,6 +33,14 @@
 // laplacian 952 / 1016; at 1024x512x512 within 0-3 %.
 #ifndef KG_TMAVEC_PDL
 #define KG_TMAVEC_PDL 1
+#endif
+// 1: consecutive sweeps alternate the direction in which their runs along
+// z (or bands of rows) are taken.  Measured on GB300 (ping-pong sweeps at
+// 512x256x256 / 512x65536, Gpts/s, fixed / alternating): FP32 gradient 356 /
+// 370, jacobi 654 / 659, wave13pt 507 / 511; BF16 gradient 521 / 544, uxx1
+// 300 / 305, jacobi 994 / 1008; the others within 0.5 %.
+#ifndef KG_TMAVEC_ALT
+#define KG_TMAVEC_ALT 1
 #endif
 
 namespace kg {
@@ -131,7 +140,7 @@ template <int I, int V, class F> __device__ __forceinline__ void for_v(F&& f)
 // points PY - 1 more times, RB rows further down each time (BY = RB PY).
 template <class Op, class N, class S, int V, int NW, int PY, int L>
 __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p, const __grid_constant__ TMaps maps,
-	int nx, int ny, int ns, int kc, int yt0, int* err, long long wait)
+	int nx, int ny, int ns, int kc, int yt0, int* err, long long wait, int rev)
 {
 	constexpr int BX = 128, LPR = BX / V, RPW = 32 / LPR, RB = NW * RPW, BY = RB * PY, NC = 32 * NW;
 	static_assert(LPR * RPW == 32, "a warp covers whole rows");
@@ -157,7 +166,8 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	Runs runs;
 	runs.xt = xt;
 	runs.yt = yt;
-	runs.kb = Op::LZ + (int)blockIdx.z * kc;
+	// rev: the runs taken from the far end of z (or of the bands) first
+	runs.kb = Op::LZ + (rev ? (int)gridDim.z - 1 - (int)blockIdx.z : (int)blockIdx.z) * kc;
 	runs.kend = kend;
 	runs.kc = kc;
 
@@ -392,6 +402,11 @@ struct TmaVecLaunch {
 			const int kc = KG_TMAVEC_ZRUNS > 0 ? (dz + zruns - 1) / zruns
 				: tma_run_length(per_sm, sms, (long long)gx * gy, dz, G::NZMAX(), 0.25, 0.0);
 			const int nz = (dz + kc - 1) / kc;
+			// consecutive sweeps walk z (the bands) in opposite directions:
+			// a sweep then starts on the planes the one before it wrote
+			// (or read) last, which are still in L2
+			static std::atomic<unsigned> sweeps{0};
+			const int rev = KG_TMAVEC_ALT ? (int)(sweeps.fetch_add(1, std::memory_order_relaxed) & 1u) : 0;
 			for (int y0 = 0; y0 < gy; y0 += 65535) {
 				dim3 grid(gx, (unsigned)min(gy - y0, 65535), (unsigned)min(nz, 65535));
 				if (KG_TMAVEC_PDL) {
@@ -408,11 +423,11 @@ struct TmaVecLaunch {
 					cfg.attrs = at;
 					cfg.numAttrs = 1;
 					e = cudaLaunchKernelEx(&cfg, tma_vec_kernel<Op, N, S, V, NW, PY, L>, op, p, maps, nx, ny, ns, kc, y0, err,
-						wait);
+						wait, rev);
 					if (e != cudaSuccess) return e;
 				} else {
 					tma_vec_kernel<Op, N, S, V, NW, PY, L><<<grid, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, kc, y0, err,
-						wait);
+						wait, rev);
 				}
 				if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			}
