@@ -768,7 +768,7 @@ def run_ir(shape=IR_SMALL, rtol=1e-10, omega=1.8, per_check=100, fp64_cap=None, 
     npts = nx * ny * ns
     out = {"shape": list(shape), "rtol": rtol, "omega": omega, "sweeps_per_check": per_check}
     kinds = kinds or [("fp64_sor", kgb200.KG_SOLVE_SOR_F64, fp64_cap),
-                      ("ir_fp32_sor", kgb200.KG_SOLVE_IR_SOR_F32, None)]
+                      ("ir_fp32_sor", kgb200.KG_SOLVE_IR_SOR_F32, args.ir_sor_cap or None)]
     for key, kind, cap in kinds:
         u = torch.zeros_like(f)
         torch.cuda.synchronize()
@@ -1113,6 +1113,8 @@ def main():
     ap.add_argument("--ir-fp64-cap", type=int, default=0, help="sweep cap of the FP64 SOR run (0: none)")
     ap.add_argument("--ir-jacobi-cap", type=int, default=0,
                     help="sweep cap of the refinement run with FP32 Jacobi sweeps (0: not run)")
+    ap.add_argument("--ir-sor-cap", type=int, default=0,
+                    help="sweep cap of the refinement run with FP32 red-black SOR sweeps (0: none)")
     args = ap.parse_args()
     args.world, args.rank, args.local_rank = dist_env()
     if args.impl == "reference":
@@ -1130,7 +1132,7 @@ def main():
     if args.workload == "ir":
         shape = tuple(int(v) for v in args.ir_shape.split(","))
         kinds = [("fp64_sor", kgb200.KG_SOLVE_SOR_F64, args.ir_fp64_cap or None),
-                 ("ir_fp32_sor", kgb200.KG_SOLVE_IR_SOR_F32, None)]
+                 ("ir_fp32_sor", kgb200.KG_SOLVE_IR_SOR_F32, args.ir_sor_cap or None)]
         if args.ir_jacobi_cap:
             kinds.append(("ir_fp32_jacobi", kgb200.KG_SOLVE_IR_JACOBI_F32, args.ir_jacobi_cap))
         res = run_ir(shape, kinds=kinds)
