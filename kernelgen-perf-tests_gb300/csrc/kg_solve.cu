@@ -74,7 +74,15 @@ __global__ void __launch_bounds__(kSX * kSY) rb_sor_kernel(T* __restrict__ u, co
 // interior keep their values (the lane writes its whole vector: no other
 // thread writes that colour's positions in this pass).
 constexpr int kSV = 4;
-__global__ void __launch_bounds__(kSX * kSY) rb_sor_split_kernel(float* __restrict__ own,
+// Resident blocks of 256 threads per SM the vector sweeps are compiled for
+// (registers capped to fit them; a few spill).  Measured at 768x768x512 (ms
+// a refinement sweep, residuals included, SOR / Jacobi): uncapped (54 and 48
+// registers) 1.098 / 0.816, 6 blocks (40) 0.930 / 0.804, 8 blocks 1.665 /
+// 0.982.
+#ifndef KG_SOLVE_MINB
+#define KG_SOLVE_MINB 6
+#endif
+__global__ void __launch_bounds__(kSX * kSY, KG_SOLVE_MINB) rb_sor_split_kernel(float* __restrict__ own,
 	const float* __restrict__ oth, const float* __restrict__ rhs, int nx, int ny, int ns, int nh, float omega,
 	int color)
 {
@@ -146,7 +154,7 @@ __global__ void __launch_bounds__(kSX * kSY) jacobi_kernel(const float* __restri
 // shuffles (the warp's end lanes load theirs).  The outer planes of e1 stay
 // 0 (positions 0 and nx - 1 of a row are written as 0, their value).  Same
 // operands, order and expression as jacobi_kernel.
-__global__ void __launch_bounds__(kSX * kSY) jacobi_vec_kernel(const float* __restrict__ e0, float* __restrict__ e1,
+__global__ void __launch_bounds__(kSX * kSY, KG_SOLVE_MINB) jacobi_vec_kernel(const float* __restrict__ e0, float* __restrict__ e1,
 	const float* __restrict__ rhs, int nx, int ny, int ns)
 {
 	const long long sy = nx, sz = (long long)nx * ny;
