@@ -175,8 +175,7 @@ kg_status kg_extra_regcount(const char* name, kg_dtype dt, int* nregs);
 /* ---- table-driven form of the same entry points ------------------------ */
 
 /* Which kernel design runs a sweep (kg_problem.engine).  AUTO: TMA_VEC for
- * KG_F32/KG_BF16/KG_F16 laplacian, divergence, gradient, uxx1, lapgsrb,
- * wave13pt, jacobi, gaussblur and gameoflife where every array and row
+ * KG_F32/KG_BF16/KG_F16 stencils (all eleven) where every array and row
  * starts on a 16-byte boundary (TMA or DIRECT otherwise); DIRECT for
  * KG_F64/KG_F64_FMA; STAGED for KG_F64_FF (TMA for its divergence and uxx1
  * where aligned).  Built: DIRECT and TMA for every floating type but

@@ -48,12 +48,13 @@ template <class N> struct Engines {
 // (where its arrays allow it, else the TMA or direct engine).  The 2D ones
 // walk bands of rows: measured at 512x65536 (Gpts/s, direct / vector TMA),
 // FP32 jacobi 362 / 616, gaussblur 255 / 479, gameoflife 355 / 604; BF16
-// 380 / 955, 258 / 627, 371 / 708.
+// 380 / 955, 258 / 627, 371 / 708.  tricubic (compute-bound) at 512x256x256:
+// FP32 95 (TMA engine) / 112, BF16 85 / 116.
 inline bool tma_vec_preferred(int stencil)
 {
 	return stencil == KG_LAPLACIAN || stencil == KG_DIVERGENCE || stencil == KG_GRADIENT ||
 		stencil == KG_UXX1 || stencil == KG_LAPGSRB || stencil == KG_WAVE13PT || stencil == KG_JACOBI ||
-		stencil == KG_GAUSSBLUR || stencil == KG_GAMEOFLIFE;
+		stencil == KG_GAUSSBLUR || stencil == KG_GAMEOFLIFE || stencil == KG_TRICUBIC || stencil == KG_TRICUBIC2;
 }
 
 inline bool tma_preferred(int stencil, int elem_bytes)

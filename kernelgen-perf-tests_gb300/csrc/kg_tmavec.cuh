@@ -293,13 +293,22 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 #ifndef KG_TMAVEC_BUDGET16
 #define KG_TMAVEC_BUDGET16 (48 * 1024)
 #endif
-// Rows of points per lane (each lane evaluates PY x V points per plane):
-// measured on GB300, two rows for 2-byte storage (BF16 wave13pt 720 -> 817
-// Gpts/s, uxx1 291 -> 334 at 1024x512x512) and one for FP32 (uxx1 279 ->
-// 242 with two; the others within 2 %).
+// Rows of points per lane (each lane evaluates PY x V points per plane; 0:
+// per op and storage size).  FP32: one (two measured: uxx1 279 -> 242, the
+// others within 2 %).  16-bit storage with the 48 KB ring budget, measured
+// on GB300 (BF16, Gpts/s at 512x256x256 or 512x65536 and 1024x512x512, two
+// rows / one): laplacian 1008 / 1116 and 1413 / 1482, divergence 738 / 780
+// and 829 / 864, uxx1 305 / 358 and 355 / 405, tricubic 116 / 121 at
+// 1024x512x512 take one; wave13pt 758 / 742 and 899 / 864, jacobi 1010 / 959,
+// gaussblur 660 / 624, gradient 545 / 537, lapgsrb 564 / 561 keep two.
 #ifndef KG_TMAVEC_PY
 #define KG_TMAVEC_PY 0
 #endif
+template <class Op> struct VecRows16 { static constexpr int v = 2; };
+template <class N> struct VecRows16<OpLaplacian<N>> { static constexpr int v = 1; };
+template <class N> struct VecRows16<OpDivergence<N>> { static constexpr int v = 1; };
+template <class N> struct VecRows16<OpUxx1<N>> { static constexpr int v = 1; };
+template <class N, bool Z> struct VecRows16<OpTricubicT<N, Z>> { static constexpr int v = 1; };
 // Runs along z per tile column (0: the TMA engine's wave-count model).
 #ifndef KG_TMAVEC_ZRUNS
 #define KG_TMAVEC_ZRUNS 0
@@ -315,7 +324,7 @@ template <class Op, class N, class S>
 struct TmaVecLaunch {
 	static constexpr bool k2d = (Op::LZ == 0 && Op::HZ == 0);
 	static constexpr int V = 16 / (int)sizeof(S), NW = 8;
-	static constexpr int PY = KG_TMAVEC_PY > 0 ? KG_TMAVEC_PY : (sizeof(S) == 2 ? 2 : 1);
+	static constexpr int PY = KG_TMAVEC_PY > 0 ? KG_TMAVEC_PY : (sizeof(S) == 2 ? VecRows16<Op>::v : 1);
 	static constexpr int BX = 128, BY = NW * (32 * V / BX) * PY;
 	static constexpr int L = TmaVecDepth<Op, S, BX, BY>::L;
 	static constexpr int kThreads = 32 * NW + 32;
