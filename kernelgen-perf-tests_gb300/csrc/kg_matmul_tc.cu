@@ -39,19 +39,28 @@
 
 namespace kg {
 
-// Tiles of 128 x TN (TN = 128: 3 stages of 64 KB; TN = 256 would take 2
-// stages of 96 KB).
-constexpr int kTcM = 128, kTcK = 32;
+constexpr int kTcM = 128;   // rows of C a CTA owns
 #ifndef KG_TC_GROUP
 #define KG_TC_GROUP 8
 #endif
-constexpr int kTcBoxA = kTcM * kTcK * 4;              // bytes of one split of A
+
+// Tiles of 128 x TN.  TN = 128: K stages of 32 (rows of 128 bytes, 128-byte
+// swizzle), 3 stages of 64 KB.  TN = 256: K stages of 16 (rows of 64 bytes,
+// 64-byte swizzle), 4 stages of 48 KB -- a third fewer operand bytes a flop
+// for the tensor cores to read from shared memory, with the stages in flight
+// of the narrower tile.  Measured on GB300 (ms, 128 / 256 columns): 2048^3
+// 0.229 / 0.214, 4096^3 1.058 / 1.083, 8192^3 5.74 / 5.29; 256 columns with
+// K stages of 32 (2 stages of 96 KB): 4096^3 1.18, 8192^3 6.40; 128 columns
+// with K stages of 16 (6 stages of 32 KB): 1.19, 6.74.
 template <int TN> struct TcShape {
 	static constexpr int N = TN;
-	static constexpr int BoxB = TN * kTcK * 4;
-	static constexpr int Stage = 2 * kTcBoxA + 2 * BoxB;   // A_hi, A_lo, B_hi, B_lo
-	static constexpr int Stages = TN == 128 ? 3 : 2;
-	static constexpr int Smem = Stages * Stage + 256 + 1024;   // + barriers, + alignment slack
+	static constexpr int K = TN == 128 ? 32 : 16;            // K elements a stage
+	static constexpr int RowBytes = K * 4;                    // = the swizzle span
+	static constexpr int BoxA = kTcM * K * 4;                 // bytes of one split of A
+	static constexpr int BoxB = TN * K * 4;
+	static constexpr int Stage = 2 * BoxA + 2 * BoxB;         // A_hi, A_lo, B_hi, B_lo
+	static constexpr int Stages = TN == 128 ? 3 : 4;
+	static constexpr int Smem = Stages * Stage + 256 + 1024;  // + barriers, + alignment slack
 };
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y)
@@ -68,13 +77,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
 // (start address, leading offset unused, stride offset, descriptor version,
 // swizzle mode).  A K step inside the 128-byte row adds its byte offset to
 // the start address; the swizzle applies to the full address.
-__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr)
+template <int ROW_BYTES>
+__device__ __forceinline__ uint64_t umma_desc_swizzled(uint32_t saddr)
 {
+	static_assert(ROW_BYTES == 128 || ROW_BYTES == 64, "128- or 64-byte swizzle");
 	uint64_t d = (uint64_t)((saddr >> 4) & 0x3fff);
 	d |= (uint64_t)1 << 16;
-	d |= (uint64_t)(1024 >> 4) << 32;
+	d |= (uint64_t)((8 * ROW_BYTES) >> 4) << 32;              // 8 rows
 	d |= (uint64_t)1 << 46;
-	d |= (uint64_t)2 << 61;
+	d |= (uint64_t)(ROW_BYTES == 128 ? 2 : 4) << 61;         // 128- or 64-byte swizzle
 	return d;
 }
 
@@ -164,7 +175,7 @@ __global__ void __launch_bounds__(256) tc_split_a(const float* __restrict__ A, f
 	__syncthreads();
 	for (int r = threadIdx.y; r < 32; r += blockDim.y) {
 		const int i = i0 + r, k = k0 + threadIdx.x;
-		if (i < nx) {
+		if (i < nx && k < kp) {
 			float h, l;
 			tf32_split(t[threadIdx.x][r], h, l);
 			hi[(size_t)i * kp + k] = h;
@@ -254,10 +265,10 @@ __global__ void __launch_bounds__(128, 1) matmul_tc_kernel(const __grid_constant
 			}
 			unsigned char* st = sm + s * kTcStage;
 			mbar_expect_tx(&full[s], kTcStage);
-			tma_load_2d(st, &m_ahi, &full[s], kb * kTcK, m0);
-			tma_load_2d(st + kTcBoxA, &m_alo, &full[s], kb * kTcK, m0);
-			tma_load_2d(st + 2 * kTcBoxA, &m_bhi, &full[s], kb * kTcK, n0);
-			tma_load_2d(st + 2 * kTcBoxA + T::BoxB, &m_blo, &full[s], kb * kTcK, n0);
+			tma_load_2d(st, &m_ahi, &full[s], kb * T::K, m0);
+			tma_load_2d(st + T::BoxA, &m_alo, &full[s], kb * T::K, m0);
+			tma_load_2d(st + 2 * T::BoxA, &m_bhi, &full[s], kb * T::K, n0);
+			tma_load_2d(st + 2 * T::BoxA + T::BoxB, &m_blo, &full[s], kb * T::K, n0);
 			issued = kb + 1;
 		}
 		if (!ok) {
@@ -279,11 +290,12 @@ __global__ void __launch_bounds__(128, 1) matmul_tc_kernel(const __grid_constant
 			tc_fence_after();
 			const uint32_t base = smem_addr(sm + s * kTcStage);
 #pragma unroll
-			for (int ks = 0; ks < kTcK / 8; ks++) {
+			for (int ks = 0; ks < T::K / 8; ks++) {
 				const uint32_t off = ks * 32;   // 8 TF32 values of K
-				const uint64_t ahi = umma_desc_sw128(base + off), alo = umma_desc_sw128(base + kTcBoxA + off);
-				const uint64_t bhi = umma_desc_sw128(base + 2 * kTcBoxA + off);
-				const uint64_t blo = umma_desc_sw128(base + 2 * kTcBoxA + T::BoxB + off);
+				constexpr int RB = T::RowBytes;
+				const uint64_t ahi = umma_desc_swizzled<RB>(base + off), alo = umma_desc_swizzled<RB>(base + T::BoxA + off);
+				const uint64_t bhi = umma_desc_swizzled<RB>(base + 2 * T::BoxA + off);
+				const uint64_t blo = umma_desc_swizzled<RB>(base + 2 * T::BoxA + T::BoxB + off);
 				umma_tf32(tmem, alo, bhi, idesc, (kb | ks) != 0);
 				umma_tf32(tmem, ahi, blo, idesc, 1);
 				umma_tf32(tmem, ahi, bhi, idesc, 1);
@@ -351,30 +363,36 @@ extern "C" kg_status kg_matmul_tc(int nx, int ny, int ns, const float* A, const 
 	cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
 	if (major != 10) return fail(KG_ENOTSUP, "matmul_tc: needs a Blackwell (sm_10x) GPU");
 	cudaStream_t st = (cudaStream_t)stream;
-	const int kp = (ny + kTcK - 1) / kTcK * kTcK;
+	const int kp = (ny + 31) / 32 * 32;   // a multiple of both shapes' K stage
 	const size_t na = (size_t)nx * kp, nb = (size_t)ns * kp;
 	float* ws = nullptr;
 	kg_status s = fail_cuda(cudaMallocAsync((void**)&ws, sizeof(float) * 2 * (na + nb), st), "matmul_tc: workspace");
 	if (s != KG_OK) return s;
 	float *ahi = ws, *alo = ws + na, *bhi = ws + 2 * na, *blo = ws + 2 * na + nb;
-	tc_split_a<<<dim3((unsigned)((nx + 31) / 32), (unsigned)(kp / 32)), dim3(32, 8), 0, st>>>(A, ahi, alo, nx, ny, kp);
+	tc_split_a<<<dim3((unsigned)((nx + 31) / 32), (unsigned)((kp + 31) / 32)), dim3(32, 8), 0, st>>>(A, ahi, alo, nx, ny, kp);
 	const long long nbl = std::min<long long>(((long long)nb + 255) / 256, 152 * 16);
 	tc_split_b<<<(unsigned)nbl, 256, 0, st>>>(B, bhi, blo, ny, ns, kp);
-	// 128-column tiles: 256-column ones (2 stages of 96 KB, a third fewer
-	// operand bytes a flop) measured slower on GB300 (4096^3: 1.18 ms against
-	// 1.06; 8192^3: 6.40 against 6.26)
-	const int tn = 128;
-	CUtensorMap maps[4];
-	cudaError_t e = cudaSuccess;
-	const float* bases[4] = {ahi, alo, bhi, blo};
-	const int rows[4] = {nx, nx, ns, ns};
-	for (int q = 0; q < 4 && e == cudaSuccess; q++)
-		e = tma_encode_2d_sw128(&maps[q], bases[q], (uint64_t)kp, (uint64_t)rows[q], kTcK, q < 2 ? kTcM : tn);
+	// 256-column tiles where their waves cost less than the 128-column ones'
+	// (a 256-column tile takes about 1.83 times a 128-column tile's time)
+	int sms = 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	sms = sms > 0 ? sms : 1;
+	const long long mt = (nx + kTcM - 1) / kTcM;
+	const long long w128 = (mt * ((ns + 127) / 128) + sms - 1) / sms, w256 = (mt * ((ns + 255) / 256) + sms - 1) / sms;
+	const bool wide = (ns + 255) / 256 <= 65535 && 1.83 * (double)w256 < (double)w128;
 	int* err = tma_error_flag();
-	if (e == cudaSuccess && !err) e = cudaErrorInvalidValue;
+	cudaError_t e = err ? cudaSuccess : cudaErrorInvalidValue;
 	if (e == cudaSuccess) {
 		auto launch = [&](auto shape) {
 			using T = decltype(shape);
+			CUtensorMap maps[4];
+			const float* bases[4] = {ahi, alo, bhi, blo};
+			const int rows[4] = {nx, nx, ns, ns};
+			for (int q = 0; q < 4; q++) {
+				cudaError_t r = tma_encode_2d_swizzled(&maps[q], bases[q], (uint64_t)kp, (uint64_t)rows[q], T::K,
+					q < 2 ? kTcM : T::N, T::RowBytes);
+				if (r != cudaSuccess) return r;
+			}
 			// the shared-memory opt-in, once per device
 			static std::atomic<bool> set[64];
 			if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
@@ -385,11 +403,11 @@ extern "C" kg_status kg_matmul_tc(int nx, int ny, int ns, const float* A, const 
 				set[dev].store(true, std::memory_order_release);
 			}
 			dim3 grid((unsigned)((nx + kTcM - 1) / kTcM), (unsigned)((ns + T::N - 1) / T::N));
-			matmul_tc_kernel<T::N><<<grid, 128, T::Smem, st>>>(maps[0], maps[1], maps[2], maps[3], C, nx, ns, kp / kTcK,
+			matmul_tc_kernel<T::N><<<grid, 128, T::Smem, st>>>(maps[0], maps[1], maps[2], maps[3], C, nx, ns, kp / T::K,
 				err, tma_wait_limit());
 			return cudaGetLastError();
 		};
-		e = launch(TcShape<128>{});
+		e = wide ? launch(TcShape<256>{}) : launch(TcShape<128>{});
 	}
 	cudaFreeAsync(ws, st);
 	return fail_cuda(e, "matmul_tc");

@@ -60,10 +60,10 @@ cudaError_t tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, const void
 
 // A rank-2 tiled map over an FP32 array of `outer` rows of `inner` elements
 // (rows contiguous, inner * 4 a multiple of 16 bytes) with boxes of
-// box_inner x box_outer elements in the 128-byte swizzle (box_inner * 4 <=
-// 128), zero fill outside the array.
-cudaError_t tma_encode_2d_sw128(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer, int box_inner,
-	int box_outer)
+// box_inner x box_outer elements in the 128- or 64-byte swizzle (box_inner *
+// 4 <= that), zero fill outside the array.
+cudaError_t tma_encode_2d_swizzled(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer, int box_inner,
+	int box_outer, int swizzle_bytes)
 {
 	cudaError_t e;
 	PFN_cuTensorMapEncodeTiled_v12000 encode = encode_fn(&e);
@@ -73,7 +73,8 @@ cudaError_t tma_encode_2d_sw128(CUtensorMap* map, const void* base, uint64_t inn
 	const cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_outer};
 	const cuuint32_t estr[2] = {1, 1};
 	CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
-		CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+		CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+		CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
 		CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 	return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }

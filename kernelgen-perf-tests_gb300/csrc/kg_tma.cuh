@@ -453,8 +453,8 @@ namespace kg {
 // device flag the kernels raise when a wait gives up.
 cudaError_t tma_encode_3d(CUtensorMap* map, CUtensorMapDataType type, const void* base, uint64_t nx,
 	uint64_t ny, uint64_t ns, int elem_bytes, int box_w, int box_h);
-cudaError_t tma_encode_2d_sw128(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer, int box_inner,
-	int box_outer);
+cudaError_t tma_encode_2d_swizzled(CUtensorMap* map, const void* base, uint64_t inner, uint64_t outer, int box_inner,
+	int box_outer, int swizzle_bytes);
 int* tma_error_flag();
 // Clock cycles a compute warp waits for its copies (kg_set_tma_wait_limit).
 long long tma_wait_limit();

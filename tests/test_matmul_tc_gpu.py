@@ -39,9 +39,11 @@ def run(nx, ny, ns, seed, c0=True):
     return got, ref, mag
 
 
-# the last shape: more than a wave of tiles, ragged in both directions
+# (2000, 100, 2600): more than a wave of 128 x 128 tiles, ragged in both
+# directions; (2000, 70, 2000): 128 x 256 tiles (one wave of them against two
+# of 128 x 128), ragged in M, N and K
 @pytest.mark.parametrize("shape", [(1, 1, 1), (7, 5, 3), (33, 17, 40), (128, 32, 128), (130, 70, 129),
-                                   (256, 96, 384), (512, 256, 256), (2000, 100, 2600)])
+                                   (256, 96, 384), (512, 256, 256), (2000, 100, 2600), (2000, 70, 2000)])
 def test_matmul_tc_matches_fp64(shape):
     got, ref, mag = run(*shape, seed=sum(shape))
     err = np.abs(got - ref)
