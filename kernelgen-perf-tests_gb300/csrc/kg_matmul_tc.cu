@@ -358,6 +358,7 @@ extern "C" kg_status kg_matmul_tc(int nx, int ny, int ns, const float* A, const 
 		return fail(KG_EINVAL, "matmul_tc: output array overlaps an input");
 	if (ny == 0) return KG_OK;   // C += nothing
 	if ((ns + 127) / 128 > 65535) return fail(KG_EINVAL, "matmul_tc: ns beyond the supported size");
+	if ((ny + 31) / 32 > 65535) return fail(KG_EINVAL, "matmul_tc: ny beyond the supported size");
 	int dev = 0, major = 0;
 	cudaGetDevice(&dev);
 	cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
