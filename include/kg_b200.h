@@ -152,7 +152,8 @@ kg_status kg_matmul(kg_dtype dt, int nx, int ny, int ns,
  * FP32 accumulation), then added to C.  FP32-accurate (about 1e-7 of the sum
  * of |A(i,k) B(k,j)|), not the k-ordered sum: not bit for bit with
  * kg_matmul.  Takes a workspace of 8 (nx + ns) kp bytes (kp: ny rounded up
- * to a multiple of 32) from the stream-ordered pool.  KG_ENOTSUP off Blackwell; a wait that gives up is
+ * to a multiple of 32) from the library's stream-ordered pool (the one
+ * kg_program_run uses; its memory stays cached between calls).  KG_ENOTSUP off Blackwell; a wait that gives up is
  * reported by kg_engine_status. */
 kg_status kg_matmul_tc(int nx, int ny, int ns, const float* A, const float* B, float* C, kg_stream_t stream);
 

@@ -35,6 +35,10 @@ void clear_error();
 
 size_t dtype_size(int dt);
 
+// The library's stream-ordered pool on the current device (kg_runtime.cu):
+// memory stays cached between calls up to a threshold.
+cudaError_t program_pool(cudaMemPool_t* out);
+
 // Tricubic programs with loop-invariant weights (kg_tricubic_pw.cu).
 size_t tricubic_pw_bytes(const kg_problem& p);
 cudaError_t tricubic_pw_precompute(const kg_problem& p, double* pw, cudaStream_t st);

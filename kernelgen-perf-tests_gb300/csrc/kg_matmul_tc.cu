@@ -367,7 +367,12 @@ extern "C" kg_status kg_matmul_tc(int nx, int ny, int ns, const float* A, const 
 	const int kp = (ny + 31) / 32 * 32;   // a multiple of both shapes' K stage
 	const size_t na = (size_t)nx * kp, nb = (size_t)ns * kp;
 	float* ws = nullptr;
-	kg_status s = fail_cuda(cudaMallocAsync((void**)&ws, sizeof(float) * 2 * (na + nb), st), "matmul_tc: workspace");
+	// from the library's pool, whose memory stays cached between calls (the
+	// device's default pool hands it back at every synchronisation)
+	cudaMemPool_t pool;
+	kg_status s = fail_cuda(program_pool(&pool), "matmul_tc: memory pool");
+	if (s != KG_OK) return s;
+	s = fail_cuda(cudaMallocFromPoolAsync((void**)&ws, sizeof(float) * 2 * (na + nb), pool, st), "matmul_tc: workspace");
 	if (s != KG_OK) return s;
 	float *ahi = ws, *alo = ws + na, *bhi = ws + 2 * na, *blo = ws + 2 * na + nb;
 	tc_split_a<<<dim3((unsigned)((nx + 31) / 32), (unsigned)((kp + 31) / 32)), dim3(32, 8), 0, st>>>(A, ahi, alo, nx, ny, kp);

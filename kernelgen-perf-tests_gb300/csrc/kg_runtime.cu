@@ -33,15 +33,15 @@ static double now_s()
 }
 
 
-// Device memory of kg_program_run: one stream-ordered pool per device, owned
-// by the library.  Allocating and freeing on the stream keeps programs that
+// Device memory of kg_program_run (and of kg_matmul_tc's workspace): one
+// stream-ordered pool per device, owned by the library.  Allocating and freeing on the stream keeps programs that
 // run concurrently on different streams from waiting on each other (cudaFree
 // waits for the whole device); up to kPoolKeep bytes stay cached between
 // calls (room for two concurrent tricubic programs of 512x256x256 with their
 // weight planes), the rest goes back to the device when a stream synchronises.
 constexpr uint64_t kPoolKeep = 48ull << 30;
 
-static cudaError_t program_pool(cudaMemPool_t* out)
+cudaError_t program_pool(cudaMemPool_t* out)
 {
 	static std::mutex m;
 	static cudaMemPool_t pools[64];
