@@ -26,7 +26,11 @@ namespace kg {
 // kTriPwEmu of every (jj, kk) row.  Measured on GB300 (512x256x256, weights
 // once + 10 sweeps, ms, all additions on the FP64 unit): 0 of 4: 85.6; 1:
 // 75.7; 2: 65.9; 3: 56.7; 4: 61.5 (10 sweeps computing the weights inline:
-// 118.7).
+// 118.7).  Between 3 and 4, x-neighbour 3 of the first 1, 2 or 3 rows jj of
+// every kk as well (tricubic / tricubic2 programs, ms, against 56.2 / 56.7):
+// 57.8 / 57.7, 60.2 / 59.8 and, with no integer additions, 56.6 / 57.0 (one
+// row), 58.3 / 58.1 (two), 60.8 / 60.4 (three): the integer multiply's extra
+// instructions cost issue slots the FP64 unit's queue would have hidden.
 #ifndef KG_PW_EMU
 #define KG_PW_EMU 3
 #endif
