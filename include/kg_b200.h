@@ -170,7 +170,8 @@ kg_status kg_whispering(kg_dtype dt, int nx, int ny, double mu, double epsilon,
 	void* e, const void* h0, void* h1, const void* u_em0, void* u_em1,
 	const void* ca, const void* cb, const void* da, const void* db, kg_stream_t stream);
 
-/* Registers per thread of the main kernel of the named test above. */
+/* Registers per thread of the main kernel of the named test above (the one that
+ * runs on 16-byte aligned arrays). */
 kg_status kg_extra_regcount(const char* name, kg_dtype dt, int* nregs);
 
 /* ---- table-driven form of the same entry points ------------------------ */

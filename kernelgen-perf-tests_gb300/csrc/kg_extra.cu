@@ -156,6 +156,95 @@ __global__ void __launch_bounds__(kMvRows, kMvMinBlocks) matvec_kernel(int nx, i
 	if (j < ny) y[j] = Conv<N, S>::to(s);
 }
 
+// FP32 with 16-byte aligned rows and x (nx a multiple of 4): the chunks reach
+// shared memory by 16-byte cp.async copies, which hold no registers, through a
+// ring of kMvaStages chunks of kMvaKC columns, so a CTA has the next chunks in
+// flight while it sums one.  Rows of kMvaLd floats: a thread reads its own row
+// 16 bytes at a time, and the eight threads of each quarter-warp then fall on
+// eight distinct groups of four banks.  Same sums in the same order as
+// matvec_kernel.  Measured on GB300 (ms, 512 x 65536 and 4096 x 65536; the
+// register-staged kernel 0.0290 and 0.195): 32 columns, 2 stages, 8 CTAs per
+// SM 0.0254 and 0.176; 3 stages (7 CTAs) 0.0268 and 0.178; 4 stages (5)
+// 0.0297 and 0.216; 64 columns, 2 stages (6) 0.0270 and 0.192; 16 columns,
+// 6 stages 0.0297 and 0.199; 8 columns, 12 stages 0.048 and 0.330.  Deeper
+// rings of narrower row segments keep more bytes in flight but spread them
+// over more DRAM pages at once.
+#ifndef KG_MVA_KC
+#define KG_MVA_KC 32
+#endif
+#ifndef KG_MVA_STAGES
+#define KG_MVA_STAGES 2
+#endif
+#ifndef KG_MVA_MINB
+#define KG_MVA_MINB 8
+#endif
+constexpr int kMvaKC = KG_MVA_KC, kMvaStages = KG_MVA_STAGES, kMvaLd = kMvaKC + 4;
+constexpr int kMvaMinBlocks = KG_MVA_MINB;   // 65536 rows of 512: one wave of 64-row CTAs on 152 SMs
+
+__device__ __forceinline__ void mv_cp16(void* dst, const void* src, int src_bytes)
+{
+	const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+
+template <class N>
+__global__ void __launch_bounds__(kMvRows, kMvaMinBlocks) matvec_ring_kernel(int nx, int ny,
+	const float* __restrict__ A, const float* __restrict__ x, float* __restrict__ y)
+{
+	__shared__ __align__(16) float tile[kMvaStages][kMvRows][kMvaLd];
+	__shared__ __align__(16) float xs[kMvaStages][kMvaKC];
+	constexpr int V = kMvaKC / 4;   // 16-byte copies a row of a chunk
+	const int t = threadIdx.x, j0 = blockIdx.x * kMvRows, j = j0 + t;
+	const int nch = (nx + kMvaKC - 1) / kMvaKC;
+	// chunk ch into its ring slot; rows past ny and columns past nx are
+	// zero-filled (no bytes read) and never summed
+	auto issue = [&](int ch) {
+		if (ch < nch) {
+			const int st = ch % kMvaStages, i0 = ch * kMvaKC;
+#pragma unroll
+			for (int q = 0; q < kMvRows * V / kMvRows; q++) {
+				const int e = t + q * kMvRows, r = e / V, c = 4 * (e % V);
+				const bool ok = j0 + r < ny && i0 + c < nx;
+				mv_cp16(&tile[st][r][c], ok ? A + (size_t)(j0 + r) * nx + i0 + c : A, ok ? 16 : 0);
+			}
+			if (t < V) {
+				const bool ok = i0 + 4 * t < nx;
+				mv_cp16(&xs[st][4 * t], ok ? x + i0 + 4 * t : x, ok ? 16 : 0);
+			}
+		}
+		asm volatile("cp.async.commit_group;" ::: "memory");   // one group per chunk, empty past the end
+	};
+#pragma unroll
+	for (int ch = 0; ch < kMvaStages - 1; ch++) issue(ch);
+	N s = N(0.0);
+	for (int ch = 0; ch < nch; ch++) {
+		issue(ch + kMvaStages - 1);   // into the slot summed in the step before (freed by its barrier)
+		asm volatile("cp.async.wait_group %0;" ::"n"(kMvaStages - 1) : "memory");
+		__syncthreads();
+		const int st = ch % kMvaStages, kc = min(kMvaKC, nx - ch * kMvaKC);
+		if (j < ny) {
+			const float4* row = reinterpret_cast<const float4*>(&tile[st][t][0]);
+			const float4* xv = reinterpret_cast<const float4*>(&xs[st][0]);
+			auto step4 = [&](int c4) {
+				const float4 a = row[c4], b = xv[c4];
+				s = s + mul_on(mkf(a.x), mkf(b.x), true);
+				s = s + mul_on(mkf(a.y), mkf(b.y), true);
+				s = s + mul_on(mkf(a.z), mkf(b.z), true);
+				s = s + mul_on(mkf(a.w), mkf(b.w), true);
+			};
+			if (kc == kMvaKC) {
+#pragma unroll
+				for (int c4 = 0; c4 < V; c4++) step4(c4);
+			} else {
+				for (int c4 = 0; c4 < kc / 4; c4++) step4(c4);
+			}
+		}
+		__syncthreads();
+	}
+	asm volatile("cp.async.wait_group 0;" ::: "memory");
+	if (j < ny) y[j] = s.v;
+}
+
 // ---- matmul/matmul.F90:56-68: C(i,j) = C(i,j) + A(i,k) * B(k,j), k = 1..ny --
 //
 // Column-major: A(i,k) at A[i + nx k], B(k,j) at B[k + ny j], C(i,j) at
@@ -227,6 +316,24 @@ __global__ void __launch_bounds__(256) sincos_kernel(size_t n, const S* __restri
 	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
 		if constexpr (std::is_same<S, double>::value) xy[i] = Conv<N, S>::to(N(sin(__ldg(x + i))) + N(cos(__ldg(y + i))));
 		else xy[i] = Conv<N, S>::to(mkf(sinf(__ldg(x + i))) + mkf(cosf(__ldg(y + i))));
+	}
+}
+
+// FP32 with 16-byte aligned arrays: four points a thread and step, so each
+// thread has 32 bytes of loads in flight instead of 8 (the scalar kernel's
+// loads in flight per SM are too few to cover HBM latency).  Same functions
+// on the same values: the same bits.
+__global__ void __launch_bounds__(256) sincos_vec_kernel(size_t nv, const float4* __restrict__ x,
+	const float4* __restrict__ y, float4* __restrict__ xy)
+{
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nv; i += (size_t)gridDim.x * blockDim.x) {
+		const float4 a = __ldg(x + i), b = __ldg(y + i);
+		float4 c;
+		c.x = (mkf(sinf(a.x)) + mkf(cosf(b.x))).v;
+		c.y = (mkf(sinf(a.y)) + mkf(cosf(b.y))).v;
+		c.z = (mkf(sinf(a.z)) + mkf(cosf(b.z))).v;
+		c.w = (mkf(sinf(a.w)) + mkf(cosf(b.w))).v;
+		xy[i] = c;
 	}
 }
 
@@ -341,8 +448,15 @@ kg_status kg_matvec(kg_dtype dt, int nx, int ny, const void* A, const void* x, v
 	return fail_cuda(by_type(dt, [&](auto nv, auto sv) {
 		using N = decltype(nv);
 		using S = decltype(sv);
-		matvec_kernel<N, S><<<(ny + kMvRows - 1) / kMvRows, kMvRows, 0, (cudaStream_t)stream>>>(
-			nx, ny, (const S*)A, (const S*)x, (S*)y);
+		const unsigned grid = (unsigned)((ny + kMvRows - 1) / kMvRows);
+		if constexpr (std::is_same<S, float>::value) {
+			if (nx >= 4 && nx % 4 == 0 && ((uintptr_t)A | (uintptr_t)x) % 16 == 0) {
+				matvec_ring_kernel<N><<<grid, kMvRows, 0, (cudaStream_t)stream>>>(nx, ny, (const float*)A,
+					(const float*)x, (float*)y);
+				return cudaGetLastError();
+			}
+		}
+		matvec_kernel<N, S><<<grid, kMvRows, 0, (cudaStream_t)stream>>>(nx, ny, (const S*)A, (const S*)x, (S*)y);
 		return cudaGetLastError();
 	}), "matvec");
 }
@@ -382,7 +496,18 @@ kg_status kg_sincos(kg_dtype dt, int nx, int ny, int ns, const void* x, const vo
 	return fail_cuda(by_type(dt, [&](auto nv, auto sv) {
 		using N = decltype(nv);
 		using S = decltype(sv);
-		sincos_kernel<N, S><<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, (const S*)x, (const S*)y, (S*)xy);
+		cudaStream_t st = (cudaStream_t)stream;
+		size_t done = 0;
+		if constexpr (std::is_same<S, float>::value) {
+			if (((uintptr_t)x | (uintptr_t)y | (uintptr_t)xy) % 16 == 0 && n >= 4) {
+				const size_t nv = n / 4;
+				sincos_vec_kernel<<<grid_for(nv, 256), 256, 0, st>>>(nv, (const float4*)x, (const float4*)y, (float4*)xy);
+				done = nv * 4;
+			}
+		}
+		if (done < n)
+			sincos_kernel<N, S><<<grid_for(n - done, 256), 256, 0, st>>>(n - done, (const S*)x + done,
+				(const S*)y + done, (S*)xy + done);
 		return cudaGetLastError();
 	}), "sincos");
 }
@@ -432,10 +557,18 @@ kg_status kg_extra_regcount(const char* name, kg_dtype dt, int* nregs)
 	by_type(dt, [&](auto nv, auto sv) {
 		using N = decltype(nv);
 		using S = decltype(sv);
-		if (!strcmp(name, "vecadd")) f = (const void*)vecadd_kernel<N, S>;
-		else if (!strcmp(name, "matvec")) f = (const void*)matvec_kernel<N, S>;
-		else if (!strcmp(name, "matmul")) f = (const void*)matmul_kernel<N, S>;
-		else if (!strcmp(name, "sincos")) f = (const void*)sincos_kernel<N, S>;
+		// the kernels that run on 16-byte aligned arrays
+		using V = typename std::conditional<std::is_same<S, double>::value, double2, float4>::type;
+		constexpr bool f32 = std::is_same<S, float>::value;
+		if (!strcmp(name, "vecadd")) f = (const void*)vecadd_vec_kernel<S, V>;
+		else if (!strcmp(name, "matvec")) {
+			if constexpr (f32) f = (const void*)matvec_ring_kernel<N>;
+			else f = (const void*)matvec_kernel<N, S>;
+		} else if (!strcmp(name, "matmul")) f = (const void*)matmul_kernel<N, S>;
+		else if (!strcmp(name, "sincos")) {
+			if constexpr (f32) f = (const void*)sincos_vec_kernel;
+			else f = (const void*)sincos_kernel<N, S>;
+		}
 		else if (!strcmp(name, "whispering")) f = (const void*)whispering_h_kernel<N, S>;
 		return cudaSuccess;
 	});

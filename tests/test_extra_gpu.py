@@ -140,3 +140,53 @@ def test_b200_extra_driver_matches_oracle(test, args):
     prints the oracle program's means."""
     _, _, im, fm = ol.extra_program(test, args)
     assert driver_lines(test, args) == ["initial mean = %f" % im, "final mean = %f" % fm]
+
+
+def _f32(rng, n):
+    return torch.from_numpy(rng.uniform(-1, 1, n).astype(np.float32)).cuda()
+
+
+@pytest.mark.parametrize("nx,ny", [(4, 1), (32, 64), (36, 65), (100, 1000), (1000, 129), (512, 65536)])
+def test_matvec_f32_ring_equals_register_staged(nx, ny):
+    """FP32 rows of a multiple of 4 with 16-byte aligned A and x take the
+    cp.async ring kernel; an x 4 bytes off alignment takes the register-staged
+    kernel.  Both sum each row in the reference's order: equal bit for bit,
+    and within FP32 rounding of the FP64 product."""
+    lib = kgb200.load()
+    rng = np.random.default_rng(nx + ny)
+    A = _f32(rng, nx * ny)
+    xb = _f32(rng, nx + 4)
+    x16, x4 = xb[:nx].clone(), xb[1:1 + nx]
+    x4.copy_(x16)
+    assert x16.data_ptr() % 16 == 0 and x4.data_ptr() % 16 == 4
+    y16 = torch.zeros(ny, dtype=torch.float32, device="cuda")
+    y4 = torch.full((ny,), 7.0, dtype=torch.float32, device="cuda")
+    kgb200.check(lib.kg_matvec(kgb200.KG_F32, nx, ny, A.data_ptr(), x16.data_ptr(), y16.data_ptr(), None))
+    kgb200.check(lib.kg_matvec(kgb200.KG_F32, nx, ny, A.data_ptr(), x4.data_ptr(), y4.data_ptr(), None))
+    g16, g4 = y16.cpu().numpy(), y4.cpu().numpy()
+    assert np.array_equal(g16.view(np.uint32), g4.view(np.uint32))
+    ref = A.double().cpu().numpy().reshape(ny, nx) @ x16.double().cpu().numpy()
+    mag = np.abs(A.double().cpu().numpy().reshape(ny, nx)) @ np.abs(x16.double().cpu().numpy())
+    assert np.all(np.abs(g16 - ref) <= nx * 2.0 ** -23 * mag + 1e-30)
+
+
+@pytest.mark.parametrize("n", [1, 4, 7, 4099, 1 << 20])
+def test_sincos_f32_vector_equals_scalar(n):
+    """Aligned FP32 sincos runs four points a thread; arrays 4 bytes off
+    alignment run the scalar kernel: the same bits, within 2 ulp-ish of FP64."""
+    lib = kgb200.load()
+    rng = np.random.default_rng(n)
+    xb, yb = _f32(rng, n + 4) * 8, _f32(rng, n + 4) * 8
+    x16, y16 = xb[:n].clone(), yb[:n].clone()
+    x4, y4 = xb[1:1 + n], yb[1:1 + n]
+    x4.copy_(x16)
+    y4.copy_(y16)
+    o16 = torch.zeros(n, dtype=torch.float32, device="cuda")
+    ob = torch.zeros(n + 4, dtype=torch.float32, device="cuda")
+    o4 = ob[1:1 + n]
+    kgb200.check(lib.kg_sincos(kgb200.KG_F32, n, 1, 1, x16.data_ptr(), y16.data_ptr(), o16.data_ptr(), None))
+    kgb200.check(lib.kg_sincos(kgb200.KG_F32, n, 1, 1, x4.data_ptr(), y4.data_ptr(), o4.data_ptr(), None))
+    g16, g4 = o16.cpu().numpy(), o4.cpu().numpy()
+    assert np.array_equal(g16.view(np.uint32), g4.view(np.uint32))
+    ref = np.sin(x16.double().cpu().numpy()) + np.cos(y16.double().cpu().numpy())
+    assert np.max(np.abs(g16 - ref)) <= 4 * 2.0 ** -23 * 2
