@@ -820,7 +820,9 @@ def run_e2e(args, dtype, lanes=E2E_LANES):
     bytes, so their copies weigh as much as their sweeps) to lanes[1] threads
     with high-priority streams: their copies run under the tricubic sweeps and
     their own sweeps are not queued behind them.  Returns the summed step
-    times."""
+    times, the copied bytes, each step's time, whether the tricubic programs
+    took their weights once, and the slowest step's per-program times (call
+    wall time and the load, compute and save phases, ms)."""
     import threading
     from concurrent.futures import ThreadPoolExecutor
 
@@ -843,7 +845,7 @@ def run_e2e(args, dtype, lanes=E2E_LANES):
     light = sorted((n for n in SUITE if n not in heavy), key=lambda nm: -(FP64_OPS_PER_PT[nm] + 2 * BYTES_PER_PT[nm]))
     if n_light == 0:
         heavy, light = heavy + light, []
-    errors, once = [], []
+    errors, once, phases = [], [], {}
 
     def lane(k, todo, lock):
         try:
@@ -854,7 +856,10 @@ def run_e2e(args, dtype, lanes=E2E_LANES):
                     name = todo.pop(0)
                 coef, arrs, _ = inputs[name]
                 p = kgb200.problem(name, dtype, shape_of(name), coef[:6], [a.ctypes.data for a in arrs])
+                w0 = time.perf_counter()
                 t = kgb200.program_run(p, NT, result_mask(name), streams[k])
+                phases[name] = [round((time.perf_counter() - w0) * 1e3, 1), round(t.load * 1e3, 1),
+                                round(t.compute * 1e3, 1), round(t.save * 1e3, 1)]
                 if name in heavy:
                     once.append(t.weights_once)
         except Exception as e:  # surfaced after the join
@@ -878,17 +883,20 @@ def run_e2e(args, dtype, lanes=E2E_LANES):
         for _ in range(max(1, min(args.warmup, 2))):
             restore()
             step()
-        dt, each = 0.0, []
+        dt, each, slowest = 0.0, [], None
         for _ in range(args.steps):
             restore()
+            phases.clear()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             step()
             torch.cuda.synchronize()
             each.append(time.perf_counter() - t0)
             dt += each[-1]
+            if each[-1] >= max(each):
+                slowest = dict(phases)
     del inputs, pristine, pairs
-    return dt, h2d, d2h, each, all(once)
+    return dt, h2d, d2h, each, all(once), slowest
 
 
 # ---- the suite's other tests (vecadd, matvec, matmul, sincos, whispering) ----
@@ -1240,11 +1248,12 @@ def main():
                     "produce the same bits)"},
     }
     if not args.no_e2e:
-        dt, h2d, d2h, each, once = run_e2e(args, dtype)
+        dt, h2d, d2h, each, once, slowest = run_e2e(args, dtype)
         dt = replica_max(dt, args.world)
         line["e2e"] = {"value": round(replica_value(args.world, pts_per_step, args.steps, dt), 4), "unit": "Gpts/s",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "step_ms": [round(t * 1e3, 1) for t in each], "tricubic_weights_once": once,
+                       "slowest_step_ms_by_program": {"fields": ["call", "load", "compute", "save"], **(slowest or {})},
                        "path": "kg_program_run per stencil (stream-ordered alloc, H2D, 10 sweeps, D2H of the "
                                "checksum arrays, free) on pinned host arrays; the 11 programs on %d host threads with a "
                                "stream each (tricubic/tricubic2 on %d normal-priority, the rest on %d high-priority)"
