@@ -76,13 +76,15 @@ __device__ __forceinline__ N vrow_value(const unsigned char* b, int row_elems, i
 	}
 }
 
-template <class Op, class N, class S, class G, int V, int VI, int RY = 0> struct VAcc {
-	static constexpr int ZS = 5;
-	const unsigned char* (*base)[ZS];   // per input and dz + z0: the lane's first column in the point's row
+// ZP: the plane of the step among the steps evaluated together (its window
+// starts ZP planes after the first step's).
+template <class Op, class N, class S, class G, int V, int VI, int RY = 0, int ZP = 0> struct VAcc {
+	static constexpr int ZS = 6;
+	const unsigned char* (*base)[ZS];   // per input and dz + z0 + ZP: the lane's first column in the point's row
 	const S* const* in;
 	long long c, sy, sz;                      // c: the lane's first point
 	__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
-		return vrow_value<N, S, V>(base[q][dz + Op::halo(q).z0], (dy + RY) * G::W(q), VI + dx + V);
+		return vrow_value<N, S, V>(base[q][dz + Op::halo(q).z0 + ZP], (dy + RY) * G::W(q), VI + dx + V);
 	}
 	__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
 		return __ldg(in[q] + c + VI + dx + (dy + RY) * sy + dz * sz);
@@ -138,7 +140,10 @@ template <int I, int V, class F> __device__ __forceinline__ void for_v(F&& f)
 // evaluates the V consecutive points from column (l mod BX/V) V of row
 // l / (BX/V) of its warp's rows, V = 16 bytes of storage, and the same
 // points PY - 1 more times, RB rows further down each time (BY = RB PY).
-template <class Op, class N, class S, int V, int NW, int PY, int L>
+// PZ = 2: the warps take the steps of a run two at a time (both planes'
+// points from one set of slot and address computations, the plane between
+// them read once for both).
+template <class Op, class N, class S, int V, int NW, int PY, int L, int PZ>
 __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p, const __grid_constant__ TMaps maps,
 	int nx, int ny, int ns, int kc, int yt0, int* err, long long wait, int rev)
 {
@@ -149,7 +154,8 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	constexpr Slots sl = Op::slots();
 	constexpr int ZS = VAcc<Op, N, S, G, V, 0, 0>::ZS;
 	static_assert(G::fits(), "tile does not fit the TMA engine");
-	static_assert(G::NZMAX() <= ZS, "at most ZS planes per window");
+	static_assert(G::NZMAX() + PZ - 1 <= ZS, "at most ZS planes per window");
+	static_assert(PZ == 1 || PZ == 2, "one or two steps at a time");
 	extern __shared__ __align__(128) unsigned char sm[];
 	uint64_t* full = reinterpret_cast<uint64_t*>(sm);
 	uint64_t* done = full + NB;
@@ -229,9 +235,13 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 #pragma unroll
 		for (int q = 0; q < G::NIN; q++) s0[q] = G::slot(q, kb);
 		const long long c0 = i0 + sy * j + sz * kb;
-		for (int s = 0; s < nsteps; s++) {
-			if (k2d) rows_valid(kb + s, valid);
-			const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[bi], ph, wait, abort));
+		for (int s = 0; s < nsteps;) {
+			const int np = (PZ == 2 && s + 1 < nsteps) ? 2 : 1;
+			// barrier index and phase of the second step
+			const int bi1 = bi + 1 == NB ? 0 : bi + 1;
+			const uint32_t ph1 = bi + 1 == NB ? ph ^ 1u : ph;
+			bool ok = __all_sync(0xffffffffu, mbar_wait(&full[bi], ph, wait, abort));
+			if (ok && np == 2) ok = __all_sync(0xffffffffu, mbar_wait(&full[bi1], ph1, wait, abort));
 			if (!ok) {
 				if (lane == 0) {
 					*abort = 1;
@@ -239,43 +249,60 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 				}
 				return;
 			}
-			const unsigned char* base[6][ZS];
+			// NP steps from one set of plane addresses: the window of step s
+			// + P is entries P .. P + NZ - 1
+			auto steps = [&](auto npc) {
+				constexpr int NP = decltype(npc)::value;
+				const unsigned char* base[6][ZS];
 #pragma unroll
-			for (int q = 0; q < G::NIN; q++) {
-				const Halo h = Op::halo(q);
+				for (int q = 0; q < G::NIN; q++) {
+					const Halo h = Op::halo(q);
 #pragma unroll
-				for (int d = 0; d < ZS; d++)
-					if (d < G::NZ(q))
-						base[q][d] = sm + G::offset(q) + G::step_slot(q, s0[q], d - h.z0) * G::PS(q) + toff[q];
-			}
-			const long long c = c0 + sz * s;
-			N o[PY][3][V];
-			for_v<0, PY>([&](auto ri) {
-				constexpr int R = decltype(ri)::value;
-				for_v<0, V>([&](auto vi) {
-					constexpr int VI = decltype(vi)::value;
-					VAcc<Op, N, S, G, V, VI, R * RB> at{base, p.in, c, sy, sz};
-					N r[3];
-					op.point(at, r);
-#pragma unroll
-					for (int q = 0; q < sl.nout; q++) o[R][q][VI] = r[q];
-				});
-			});
-			// this warp is done with the step's planes
-			__syncwarp();
-			if (lane == 0) mbar_arrive(&done[bi]);
-#pragma unroll
-			for (int r = 0; r < PY; r++)
-				if (valid[r]) {
-#pragma unroll
-					for (int q = 0; q < sl.nout; q++) vstore<N, S, V>(p.out[q] + c + r * RB * sy, o[r][q], valid[r]);
+					for (int d = 0; d < ZS; d++)
+						if (d < G::NZ(q) + NP - 1)
+							base[q][d] = sm + G::offset(q) + G::step_slot(q, s0[q], d - h.z0) * G::PS(q) + toff[q];
 				}
-			if (++bi == NB) {
-				bi = 0;
-				ph ^= 1;
-			}
+				N o[NP][PY][3][V];
+				for_v<0, NP>([&](auto pi) {
+					constexpr int P = decltype(pi)::value;
+					for_v<0, PY>([&](auto ri) {
+						constexpr int R = decltype(ri)::value;
+						for_v<0, V>([&](auto vi) {
+							constexpr int VI = decltype(vi)::value;
+							VAcc<Op, N, S, G, V, VI, R * RB, P> at{base, p.in, c0 + sz * (s + P), sy, sz};
+							N r[3];
+							op.point(at, r);
 #pragma unroll
-			for (int q = 0; q < G::NIN; q++) s0[q] = G::step_slot(q, s0[q], 1);
+							for (int q = 0; q < sl.nout; q++) o[P][R][q][VI] = r[q];
+						});
+					});
+				});
+				// this warp is done with the steps' planes
+				__syncwarp();
+				if (lane == 0) {
+					mbar_arrive(&done[bi]);
+					if (NP == 2) mbar_arrive(&done[bi1]);
+				}
+#pragma unroll
+				for (int P = 0; P < NP; P++) {
+					if (k2d) rows_valid(kb + s + P, valid);
+					const long long c = c0 + sz * (s + P);
+#pragma unroll
+					for (int r = 0; r < PY; r++)
+						if (valid[r]) {
+#pragma unroll
+							for (int q = 0; q < sl.nout; q++)
+								vstore<N, S, V>(p.out[q] + c + r * RB * sy, o[P][r][q], valid[r]);
+						}
+				}
+			};
+			if (np == 2) steps(std::integral_constant<int, PZ>{});
+			else steps(std::integral_constant<int, 1>{});
+			s += np;
+			bi = np == 2 ? (bi1 + 1 == NB ? 0 : bi1 + 1) : bi1;
+			ph = np == 2 ? (bi1 + 1 == NB ? ph1 ^ 1u : ph1) : ph1;
+#pragma unroll
+			for (int q = 0; q < G::NIN; q++) s0[q] = G::step_slot(q, s0[q], np);
 		}
 	}
 }
@@ -309,6 +336,22 @@ template <class N> struct VecRows16<OpLaplacian<N>> { static constexpr int v = 1
 template <class N> struct VecRows16<OpDivergence<N>> { static constexpr int v = 1; };
 template <class N> struct VecRows16<OpUxx1<N>> { static constexpr int v = 1; };
 template <class N, bool Z> struct VecRows16<OpTricubicT<N, Z>> { static constexpr int v = 1; };
+// Steps a compute warp takes at a time (0: per op; 1 or 2 for all).
+#ifndef KG_TMAVEC_PZ
+#define KG_TMAVEC_PZ 0
+#endif
+// Two at a time pays where a point reads many rows of the planes around it:
+// the rows of the planes the two steps share are loaded once.  Measured on
+// GB300 (Gpts/s at 512x256x256 and 1024x512x512, one step / two): FP32
+// lapgsrb 356 / 442 and 382 / 485 (the same gain on a second box); FP32
+// laplacian 734 / 785 on one box and 786 / 769 on another, the others within
+// the boxes' spread or slower, tricubic 121 / 116, uxx1 268 / 145; with 16-bit
+// storage every stencil slower (BF16 laplacian 1149 / 1005, lapgsrb 517 /
+// 445: the second step's registers cost resident CTAs, and capping the
+// registers for four CTAs per SM still left laplacian at 1112 and divergence
+// at 761 against 780).
+template <class Op, class S> struct VecSteps { static constexpr int v = 1; };
+template <class N> struct VecSteps<OpLapgsrb<N>, float> { static constexpr int v = 2; };
 // Runs along z per tile column (0: the TMA engine's wave-count model).
 #ifndef KG_TMAVEC_ZRUNS
 #define KG_TMAVEC_ZRUNS 0
@@ -327,6 +370,7 @@ struct TmaVecLaunch {
 	static constexpr int PY = KG_TMAVEC_PY > 0 ? KG_TMAVEC_PY : (sizeof(S) == 2 ? VecRows16<Op>::v : 1);
 	static constexpr int BX = 128, BY = NW * (32 * V / BX) * PY;
 	static constexpr int L = TmaVecDepth<Op, S, BX, BY>::L;
+	static constexpr int PZ = KG_TMAVEC_PZ > 0 ? KG_TMAVEC_PZ : VecSteps<Op, S>::v;
 	static constexpr int kThreads = 32 * NW + 32;
 	using G = TGeo<Op, S, BX, BY, L>;
 	static constexpr bool reach_ok() {
@@ -338,7 +382,7 @@ struct TmaVecLaunch {
 	// along z, 2D ops down bands of BY rows)
 	static constexpr bool built = (sizeof(S) == 4 || sizeof(S) == 2) && reach_ok();
 	static const void* func() {
-		if constexpr (built) return (const void*)tma_vec_kernel<Op, N, S, V, NW, PY, L>;
+		if constexpr (built) return (const void*)tma_vec_kernel<Op, N, S, V, NW, PY, L, PZ>;
 		else return nullptr;
 	}
 
@@ -380,7 +424,7 @@ struct TmaVecLaunch {
 					return e;
 				int b = 0, n = 0;
 				if ((e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-				if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, tma_vec_kernel<Op, N, S, V, NW, PY, L>, kThreads, smem)) != cudaSuccess)
+				if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, tma_vec_kernel<Op, N, S, V, NW, PY, L, PZ>, kThreads, smem)) != cudaSuccess)
 					return e;
 				occ = ((b > 0 ? b : 1) << 16) | (n & 0xffff);
 				occ_of[dev].store(occ, std::memory_order_release);
@@ -431,11 +475,11 @@ struct TmaVecLaunch {
 					at[0].val.programmaticStreamSerializationAllowed = 1;
 					cfg.attrs = at;
 					cfg.numAttrs = 1;
-					e = cudaLaunchKernelEx(&cfg, tma_vec_kernel<Op, N, S, V, NW, PY, L>, op, p, maps, nx, ny, ns, kc, y0, err,
+					e = cudaLaunchKernelEx(&cfg, tma_vec_kernel<Op, N, S, V, NW, PY, L, PZ>, op, p, maps, nx, ny, ns, kc, y0, err,
 						wait, rev);
 					if (e != cudaSuccess) return e;
 				} else {
-					tma_vec_kernel<Op, N, S, V, NW, PY, L><<<grid, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, kc, y0, err,
+					tma_vec_kernel<Op, N, S, V, NW, PY, L, PZ><<<grid, kThreads, smem, st>>>(op, p, maps, nx, ny, ns, kc, y0, err,
 						wait, rev);
 				}
 				if ((e = cudaGetLastError()) != cudaSuccess) return e;
