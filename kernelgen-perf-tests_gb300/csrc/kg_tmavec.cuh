@@ -343,15 +343,16 @@ template <class N, bool Z> struct VecRows16<OpTricubicT<N, Z>> { static constexp
 // Two at a time pays where a point reads many rows of the planes around it:
 // the rows of the planes the two steps share are loaded once.  Measured on
 // GB300 (Gpts/s at 512x256x256 and 1024x512x512, one step / two): FP32
-// lapgsrb 356 / 442 and 382 / 485 (the same gain on a second box); FP32
-// laplacian 734 / 785 on one box and 786 / 769 on another, the others within
-// the boxes' spread or slower, tricubic 121 / 116, uxx1 268 / 145; with 16-bit
-// storage every stencil slower (BF16 laplacian 1149 / 1005, lapgsrb 517 /
-// 445: the second step's registers cost resident CTAs, and capping the
-// registers for four CTAs per SM still left laplacian at 1112 and divergence
-// at 761 against 780).
-template <class Op, class S> struct VecSteps { static constexpr int v = 1; };
+// lapgsrb 356 / 442 and 382 / 485 (the same gain on every box); FP32
+// laplacian at 512x256x256 734 / 785, 733 / 790 and 786 / 769 on three
+// boxes (two steps steadier), 1024x512x512 within 1 %; the others within the
+// boxes' spread or slower (uxx1 268 / 145, tricubic 121 / 116).  With 16-bit
+// storage every stencil was slower, the second step's registers costing
+// resident CTAs (BF16 laplacian 1149 / 1005; 1112 with the registers capped
+// for four CTAs per SM, divergence 761 against 780; lapgsrb with one row of
+// points a lane instead of two 557 / 485).
 template <class N> struct VecSteps<OpLapgsrb<N>, float> { static constexpr int v = 2; };
+template <class N> struct VecSteps<OpLaplacian<N>, float> { static constexpr int v = 2; };
 // Runs along z per tile column (0: the TMA engine's wave-count model).
 #ifndef KG_TMAVEC_ZRUNS
 #define KG_TMAVEC_ZRUNS 0
