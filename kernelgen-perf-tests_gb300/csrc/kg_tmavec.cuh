@@ -351,6 +351,7 @@ template <class N, bool Z> struct VecRows16<OpTricubicT<N, Z>> { static constexp
 // resident CTAs (BF16 laplacian 1149 / 1005; 1112 with the registers capped
 // for four CTAs per SM, divergence 761 against 780; lapgsrb with one row of
 // points a lane instead of two 557 / 485).
+template <class Op, class S> struct VecSteps { static constexpr int v = 1; };
 template <class N> struct VecSteps<OpLapgsrb<N>, float> { static constexpr int v = 2; };
 template <class N> struct VecSteps<OpLaplacian<N>, float> { static constexpr int v = 2; };
 // Runs along z per tile column (0: the TMA engine's wave-count model).
