@@ -77,9 +77,9 @@ __device__ __forceinline__ N vrow_value(const unsigned char* b, int row_elems, i
 }
 
 // ZP: the plane of the step among the steps evaluated together (its window
-// starts ZP planes after the first step's).
-template <class Op, class N, class S, class G, int V, int VI, int RY = 0, int ZP = 0> struct VAcc {
-	static constexpr int ZS = 6;
+// starts ZP planes after the first step's); ZS_: window entries per input.
+template <class Op, class N, class S, class G, int V, int VI, int RY = 0, int ZP = 0, int ZS_ = 5> struct VAcc {
+	static constexpr int ZS = ZS_;
 	const unsigned char* (*base)[ZS];   // per input and dz + z0 + ZP: the lane's first column in the point's row
 	const S* const* in;
 	long long c, sy, sz;                      // c: the lane's first point
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 	using G = TGeo<Op, S, BX, BY, L>;
 	constexpr int NB = G::NB;
 	constexpr Slots sl = Op::slots();
-	constexpr int ZS = VAcc<Op, N, S, G, V, 0, 0>::ZS;
+	constexpr int ZS = 4 + PZ;   // window entries per input: the planes of PZ steps
 	static_assert(G::fits(), "tile does not fit the TMA engine");
 	static_assert(G::NZMAX() + PZ - 1 <= ZS, "at most ZS planes per window");
 	static_assert(PZ == 1 || PZ == 2, "one or two steps at a time");
@@ -235,8 +235,58 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 #pragma unroll
 		for (int q = 0; q < G::NIN; q++) s0[q] = G::slot(q, kb);
 		const long long c0 = i0 + sy * j + sz * kb;
+		if constexpr (PZ == 1) {
+		for (int s = 0; s < nsteps; s++) {
+			if (k2d) rows_valid(kb + s, valid);
+			const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[bi], ph, wait, abort));
+			if (!ok) {
+				if (lane == 0) {
+					*abort = 1;
+					atomicExch(err, 1);
+				}
+				return;
+			}
+			const unsigned char* base[6][ZS];
+#pragma unroll
+			for (int q = 0; q < G::NIN; q++) {
+				const Halo h = Op::halo(q);
+#pragma unroll
+				for (int d = 0; d < ZS; d++)
+					if (d < G::NZ(q))
+						base[q][d] = sm + G::offset(q) + G::step_slot(q, s0[q], d - h.z0) * G::PS(q) + toff[q];
+			}
+			const long long c = c0 + sz * s;
+			N o[PY][3][V];
+			for_v<0, PY>([&](auto ri) {
+				constexpr int R = decltype(ri)::value;
+				for_v<0, V>([&](auto vi) {
+					constexpr int VI = decltype(vi)::value;
+					VAcc<Op, N, S, G, V, VI, R * RB, 0, ZS> at{base, p.in, c, sy, sz};
+					N r[3];
+					op.point(at, r);
+#pragma unroll
+					for (int q = 0; q < sl.nout; q++) o[R][q][VI] = r[q];
+				});
+			});
+			// this warp is done with the step's planes
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&done[bi]);
+#pragma unroll
+			for (int r = 0; r < PY; r++)
+				if (valid[r]) {
+#pragma unroll
+					for (int q = 0; q < sl.nout; q++) vstore<N, S, V>(p.out[q] + c + r * RB * sy, o[r][q], valid[r]);
+				}
+			if (++bi == NB) {
+				bi = 0;
+				ph ^= 1;
+			}
+#pragma unroll
+			for (int q = 0; q < G::NIN; q++) s0[q] = G::step_slot(q, s0[q], 1);
+		}
+		} else {
 		for (int s = 0; s < nsteps;) {
-			const int np = (PZ == 2 && s + 1 < nsteps) ? 2 : 1;
+			const int np = s + 1 < nsteps ? 2 : 1;
 			// barrier index and phase of the second step
 			const int bi1 = bi + 1 == NB ? 0 : bi + 1;
 			const uint32_t ph1 = bi + 1 == NB ? ph ^ 1u : ph;
@@ -269,7 +319,7 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 						constexpr int R = decltype(ri)::value;
 						for_v<0, V>([&](auto vi) {
 							constexpr int VI = decltype(vi)::value;
-							VAcc<Op, N, S, G, V, VI, R * RB, P> at{base, p.in, c0 + sz * (s + P), sy, sz};
+							VAcc<Op, N, S, G, V, VI, R * RB, P, ZS> at{base, p.in, c0 + sz * (s + P), sy, sz};
 							N r[3];
 							op.point(at, r);
 #pragma unroll
@@ -296,13 +346,14 @@ __global__ void __launch_bounds__(32 * NW + 32) tma_vec_kernel(Op op, Ptrs<S> p,
 						}
 				}
 			};
-			if (np == 2) steps(std::integral_constant<int, PZ>{});
+			if (np == 2) steps(std::integral_constant<int, 2>{});
 			else steps(std::integral_constant<int, 1>{});
 			s += np;
 			bi = np == 2 ? (bi1 + 1 == NB ? 0 : bi1 + 1) : bi1;
 			ph = np == 2 ? (bi1 + 1 == NB ? ph1 ^ 1u : ph1) : ph1;
 #pragma unroll
 			for (int q = 0; q < G::NIN; q++) s0[q] = G::step_slot(q, s0[q], np);
+		}
 		}
 	}
 }
