@@ -222,6 +222,54 @@ __device__ __forceinline__ FF operator-(FF a, FF b) { return mkf(a.v - b.v); }
 __device__ __forceinline__ FF operator*(FF a, FF b) { return mkf(a.v * b.v); }
 __device__ __forceinline__ FF operator/(FF a, FF b) { return mkf(a.v / b.v); }
 
+// H16<S>: a BF16 or FP16 value still in its half of a 32-bit word of a
+// loaded vector, as the vector TMA engine reads 16-bit storage.  Used as FF
+// it is widened (a shift or mask for BF16, a conversion for FP16); added to
+// an FP32 sum it needs no widening at all: GB300's mixed-precision add takes
+// the 16-bit operand from its half of the register (add.rn.f32.bf16 /
+// add.rn.f32.f16, the exact sum of the widened value and the FP32 operand
+// rounded to nearest: the same bits as widening first).
+template <class S> struct H16 {
+	uint32_t w;
+	int hi;   // 1: the upper 16 bits
+	__device__ __forceinline__ operator FF() const {
+		if constexpr (std::is_same<S, __nv_bfloat16>::value)
+			return mkf(__uint_as_float(hi ? (w & 0xffff0000u) : (w << 16)));
+		else
+			return mkf(__half2float(__ushort_as_half((unsigned short)(hi ? (w >> 16) : (w & 0xffffu)))));
+	}
+};
+template <class T> struct IsH16 : std::false_type {};
+template <class S> struct IsH16<H16<S>> : std::true_type {};
+
+// acc + x with x taken from its half-word by the mixed-precision add
+template <class S> __device__ __forceinline__ FF add_h16(FF acc, H16<S> x)
+{
+	float d;
+	if constexpr (std::is_same<S, __nv_bfloat16>::value) {
+		if (x.hi) asm("{ .reg .b16 l, h; mov.b32 {l, h}, %1; add.rn.f32.bf16 %0, h, %2; }" : "=f"(d) : "r"(x.w), "f"(acc.v));
+		else asm("{ .reg .b16 l, h; mov.b32 {l, h}, %1; add.rn.f32.bf16 %0, l, %2; }" : "=f"(d) : "r"(x.w), "f"(acc.v));
+	} else {
+		if (x.hi) asm("{ .reg .b16 l, h; mov.b32 {l, h}, %1; add.rn.f32.f16 %0, h, %2; }" : "=f"(d) : "r"(x.w), "f"(acc.v));
+		else asm("{ .reg .b16 l, h; mov.b32 {l, h}, %1; add.rn.f32.f16 %0, l, %2; }" : "=f"(d) : "r"(x.w), "f"(acc.v));
+	}
+	return mkf(d);
+}
+__device__ __forceinline__ FF to_ff(FF x) { return x; }
+template <class S> __device__ __forceinline__ FF to_ff(H16<S> x) { return FF(x); }
+// Every other operation widens the 16-bit operand first and is the FF
+// operation itself, so nvcc forms (and contracts) exactly the expression it
+// forms with FF operands.
+template <class S> __device__ __forceinline__ FF operator+(H16<S> a, H16<S> b) { return FF(a) + FF(b); }
+template <class S> __device__ __forceinline__ FF operator+(H16<S> a, FF b) { return FF(a) + b; }
+template <class S> __device__ __forceinline__ FF operator+(FF a, H16<S> b) { return a + FF(b); }
+template <class S> __device__ __forceinline__ FF operator-(H16<S> a, H16<S> b) { return FF(a) - FF(b); }
+template <class S> __device__ __forceinline__ FF operator-(H16<S> a, FF b) { return FF(a) - b; }
+template <class S> __device__ __forceinline__ FF operator-(FF a, H16<S> b) { return a - FF(b); }
+template <class S> __device__ __forceinline__ FF operator*(H16<S> a, H16<S> b) { return FF(a) * FF(b); }
+template <class S> __device__ __forceinline__ FF operator*(H16<S> a, FF b) { return FF(a) * b; }
+template <class S> __device__ __forceinline__ FF operator*(FF a, H16<S> b) { return a * FF(b); }
+
 // FF2: an FP64 value carried as an unevaluated sum hi + lo of two FP32
 // numbers ("float-float"), computed on the FP32 pipes with error-free
 // transformations: TwoSum (Knuth) for additions, the FMA product error for

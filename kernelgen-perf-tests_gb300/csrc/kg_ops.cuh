@@ -42,6 +42,8 @@ template <class N> __device__ __forceinline__ N pm(N a, N b)
 	if constexpr (std::is_same<N, SD>::value) return SD(se_mul(a.v, b.v));
 	else return a * b;
 }
+template <class S> __device__ __forceinline__ FF pm(FF a, H16<S> b) { return a * FF(b); }
+template <class S> __device__ __forceinline__ FF pm(H16<S> a, FF b) { return FF(a) * b; }
 
 // pdiv(a, b): a / b; in strict FP64 formed by the exact digit-recurrence
 // division on the integer and FP32 pipes (se_div; the same bits as the FP64
@@ -84,9 +86,24 @@ template <int I, int K, class... T> __device__ __forceinline__ double nsum_sd(do
 	return nsum_sd<I + 1, K>(acc, rest...);
 }
 
-template <int K = 0, class N, class... T> __device__ __forceinline__ N nsum(N a, T... rest)
+// FF sums with 16-bit terms (the vector engine's BF16/FP16 reads): each
+// 16-bit term joins by the mixed-precision add (no widening instruction) where
+// the sum so far cannot be a product that nvcc would contract with the
+// addition (any sum after the first addition, or a first term read from
+// storage); otherwise the FF addition, as the expression is written.
+template <bool SAFE> __device__ __forceinline__ FF nsum_h16(FF acc) { return acc; }
+template <bool SAFE, class X, class... T> __device__ __forceinline__ FF nsum_h16(FF acc, X x, T... rest)
 {
-	if constexpr (std::is_same<N, SD>::value) {
+	if constexpr (IsH16<X>::value && SAFE) acc = add_h16(acc, x);
+	else acc = acc + to_ff(x);
+	return nsum_h16<true>(acc, rest...);
+}
+
+template <int K = 0, class N, class... T> __device__ __forceinline__ auto nsum(N a, T... rest)
+{
+	if constexpr (IsH16<N>::value || (IsH16<T>::value || ...)) {
+		return nsum_h16<IsH16<N>::value>(to_ff(a), rest...);
+	} else if constexpr (std::is_same<N, SD>::value) {
 		return SD(nsum_sd<0, K>(a.v, rest...));
 	} else if constexpr (std::is_same<N, FF2>::value) {
 		float s = a.hi, e = a.lo;
@@ -264,9 +281,9 @@ template <class N, bool FROM_ZERO> struct OpTricubicT {
 	template <class A> __device__ __forceinline__ void point(const A& at, N* o) const {
 		const int u0 = 0, pa = 1, pb = 2, pc = 3;
 		N wa[4], wb[4], wc[4];
-		tricubic_weights(at(pa, 0, 0, 0), wa);
-		tricubic_weights(at(pb, 0, 0, 0), wb);
-		tricubic_weights(at(pc, 0, 0, 0), wc);
+		tricubic_weights(N(at(pa, 0, 0, 0)), wa);
+		tricubic_weights(N(at(pb, 0, 0, 0)), wb);
+		tricubic_weights(N(at(pc, 0, 0, 0)), wc);
 		if constexpr (std::is_same<N, SD>::value) {
 			// Strict FP64: the same products and sum, but a share of the 128
 			// products (wa*wb)*wc and (...)*u0 is formed by the exact integer

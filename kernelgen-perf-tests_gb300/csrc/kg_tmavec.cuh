@@ -59,18 +59,20 @@ __device__ __forceinline__ S vrow_load(const unsigned char* b, int row_elems, in
 	return pk.v[x % V];
 }
 
-// The same value as FP32 arithmetic reads it.  BF16 is the upper half of
-// an FP32 pattern: the element is taken from the 16-byte vector's 32-bit
-// word by one shift or mask (the conversion, exactly), no 16-bit extract.
+// The value as FP32 arithmetic reads it.  16-bit storage: the element stays
+// in its half of the 16-byte vector's 32-bit word (H16): sums take it from
+// there by the mixed-precision add, every other use widens it (for BF16, the
+// upper half of an FP32 pattern, by one shift or mask: the conversion,
+// exactly).
 template <class N, class S, int V>
-__device__ __forceinline__ N vrow_value(const unsigned char* b, int row_elems, int x)
+__device__ __forceinline__ auto vrow_value(const unsigned char* b, int row_elems, int x)
 {
-	if constexpr (std::is_same<S, __nv_bfloat16>::value) {
+	if constexpr (sizeof(S) == 2) {
 		const int chunk = x / V - 1;
 		const uint4 q = *reinterpret_cast<const uint4*>(b + (row_elems + chunk * V) * (int)sizeof(S));
 		const int e = x % V;
 		const uint32_t w = e / 2 == 0 ? q.x : e / 2 == 1 ? q.y : e / 2 == 2 ? q.z : q.w;
-		return mkf(__uint_as_float(e % 2 ? (w & 0xffff0000u) : (w << 16)));
+		return H16<S>{w, e % 2};
 	} else {
 		return Conv<N, S>::from(vrow_load<S, V>(b, row_elems, x));
 	}
@@ -83,7 +85,7 @@ template <class Op, class N, class S, class G, int V, int VI, int RY = 0, int ZP
 	const unsigned char* (*base)[ZS];   // per input and dz + z0 + ZP: the lane's first column in the point's row
 	const S* const* in;
 	long long c, sy, sz;                      // c: the lane's first point
-	__device__ __forceinline__ N operator()(int q, int dx, int dy, int dz) const {
+	__device__ __forceinline__ auto operator()(int q, int dx, int dy, int dz) const {
 		return vrow_value<N, S, V>(base[q][dz + Op::halo(q).z0 + ZP], (dy + RY) * G::W(q), VI + dx + V);
 	}
 	__device__ __forceinline__ S raw(int q, int dx, int dy, int dz) const {
