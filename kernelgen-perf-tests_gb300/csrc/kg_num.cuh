@@ -255,15 +255,30 @@ template <class S> __device__ __forceinline__ FF add_h16(FF acc, H16<S> x)
 	}
 	return mkf(d);
 }
+// x - c with x taken from its half-word by the mixed-precision subtraction
+template <class S> __device__ __forceinline__ FF sub_h16(H16<S> x, FF c)
+{
+	float d;
+	if constexpr (std::is_same<S, __nv_bfloat16>::value) {
+		if (x.hi) asm("{ .reg .b16 l, h; mov.b32 {l, h}, %1; sub.rn.f32.bf16 %0, h, %2; }" : "=f"(d) : "r"(x.w), "f"(c.v));
+		else asm("{ .reg .b16 l, h; mov.b32 {l, h}, %1; sub.rn.f32.bf16 %0, l, %2; }" : "=f"(d) : "r"(x.w), "f"(c.v));
+	} else {
+		if (x.hi) asm("{ .reg .b16 l, h; mov.b32 {l, h}, %1; sub.rn.f32.f16 %0, h, %2; }" : "=f"(d) : "r"(x.w), "f"(c.v));
+		else asm("{ .reg .b16 l, h; mov.b32 {l, h}, %1; sub.rn.f32.f16 %0, l, %2; }" : "=f"(d) : "r"(x.w), "f"(c.v));
+	}
+	return mkf(d);
+}
 __device__ __forceinline__ FF to_ff(FF x) { return x; }
 template <class S> __device__ __forceinline__ FF to_ff(H16<S> x) { return FF(x); }
+// The sum or difference of two 16-bit values (no product for nvcc to
+// contract with it): one operand widened, the other taken from its half-word.
 // Every other operation widens the 16-bit operand first and is the FF
 // operation itself, so nvcc forms (and contracts) exactly the expression it
 // forms with FF operands.
-template <class S> __device__ __forceinline__ FF operator+(H16<S> a, H16<S> b) { return FF(a) + FF(b); }
+template <class S> __device__ __forceinline__ FF operator+(H16<S> a, H16<S> b) { return add_h16(FF(a), b); }
 template <class S> __device__ __forceinline__ FF operator+(H16<S> a, FF b) { return FF(a) + b; }
 template <class S> __device__ __forceinline__ FF operator+(FF a, H16<S> b) { return a + FF(b); }
-template <class S> __device__ __forceinline__ FF operator-(H16<S> a, H16<S> b) { return FF(a) - FF(b); }
+template <class S> __device__ __forceinline__ FF operator-(H16<S> a, H16<S> b) { return sub_h16(a, FF(b)); }
 template <class S> __device__ __forceinline__ FF operator-(H16<S> a, FF b) { return FF(a) - b; }
 template <class S> __device__ __forceinline__ FF operator-(FF a, H16<S> b) { return a - FF(b); }
 template <class S> __device__ __forceinline__ FF operator*(H16<S> a, H16<S> b) { return FF(a) * FF(b); }
