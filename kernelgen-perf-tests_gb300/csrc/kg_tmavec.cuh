@@ -396,10 +396,10 @@ template <class N, bool Z> struct VecRows16<OpTricubicT<N, Z>> { static constexp
 // Two at a time pays where a point reads many rows of the planes around it:
 // the rows of the planes the two steps share are loaded once.  Measured on
 // GB300 (Gpts/s at 512x256x256 and 1024x512x512, one step / two): FP32
-// lapgsrb 356 / 442 and 382 / 485 (the same gain on every box); FP32
-// laplacian at 512x256x256 734 / 785, 733 / 790 and 786 / 769 on three
-// boxes (two steps steadier), 1024x512x512 within 1 %; the others within the
-// boxes' spread or slower (uxx1 268 / 145, tricubic 121 / 116).  With 16-bit
+// lapgsrb 356 / 442 and 382 / 485 (the same gain on every GPU measured);
+// FP32 laplacian at 512x256x256 734 / 785, 733 / 790 and 786 / 769 on three
+// GPUs (two steps steadier), 1024x512x512 within 1 %; the others within the
+// spread between GPUs or slower (uxx1 268 / 145, tricubic 121 / 116).  With 16-bit
 // storage every stencil was slower, the second step's registers costing
 // resident CTAs (BF16 laplacian 1149 / 1005; 1112 with the registers capped
 // for four CTAs per SM, divergence 761 against 780; lapgsrb with one row of
